@@ -1,0 +1,211 @@
+/*
+ * atm_capi.h -- C ABI of the GB300-native ATMMetaForce evaluation path.
+ *
+ * Plain C types only (pointers, sizes, doubles); every function returns an
+ * ATM_* status code (0 = success) and atm_last_error() gives the message of the
+ * most recent failure on the calling thread.  Reference citations are paths in
+ * the reference plugin (Gallicchio-Lab/openmm-atmmetaforce-plugin) of the
+ * interface each entry point stands in for.
+ *
+ * Object model (mirrors OpenMM's, which the reference plugs into):
+ *   atm_force_t      ATMMetaForce                   openmmapi/include/ATMMetaForce.h:54-315
+ *   atm_nonbonded_t  the inner NonbondedForce the ATM force re-evaluates
+ *                    (ATMMetaForceImpl.cpp:96-110 clones it into the inner systems)
+ *   atm_system_t     System: particles, default box, forces (owned, as in OpenMM)
+ *   atm_context_t    one evaluation context on one GPU (ATMMetaForceImpl +
+ *                    CalcATMMetaForceKernel, ATMMetaForceKernels.h:15-59)
+ *   atm_batch_t      R replicas (systems of any sizes) evaluated by one CUDA graph
+ */
+#ifndef ATM_CAPI_H
+#define ATM_CAPI_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define ATM_OK 0
+#define ATM_ERR_INVALID_ARGUMENT 1 /* bad value or null pointer */
+#define ATM_ERR_INDEX 2            /* index out of range (ASSERT_VALID_INDEX, ATMMetaForce.cpp:18,27) */
+#define ATM_ERR_STATE 3            /* call not valid in the current state */
+#define ATM_ERR_CUDA 4             /* CUDA runtime / cuFFT failure */
+#define ATM_ERR_UNSUPPORTED 5      /* feature outside this implementation */
+#define ATM_ERR_OVERFLOW 6         /* device-side capacity exceeded and not recoverable */
+#define ATM_ERR_PARSE 7            /* malformed or unsupported XML (ATMMetaForceProxy.cpp:44) */
+#define ATM_ERR_GROUP 8            /* ATM group among the variable groups (ATMMetaForceImpl.cpp:78-79) */
+#define ATM_ERR_PARTICLES 9        /* particle count/index changed (ReferenceATMMetaForceKernels.cpp:147-154) */
+
+/* ---- nonbonded methods (OpenMM NonbondedForce::NonbondedMethod numbering) -- */
+#define ATM_NB_NOCUTOFF 0
+#define ATM_NB_CUTOFF_NONPERIODIC 1
+#define ATM_NB_CUTOFF_PERIODIC 2
+#define ATM_NB_PME 4
+
+/* ---- global parameter indices (ATMMetaForce.h:151-218) -------------------- */
+#define ATM_LAMBDA1 0
+#define ATM_LAMBDA2 1
+#define ATM_ALPHA 2
+#define ATM_U0 3
+#define ATM_W0 4
+#define ATM_UMAX 5
+#define ATM_UBCORE 6
+#define ATM_ACORE 7
+#define ATM_DIRECTION 8
+#define ATM_NUM_GLOBALS 9
+
+/* ---- per-replica result record (atm_batch_get_results) -------------------- */
+#define ATM_RES_ENERGY 0      /* e0 + W, the ATMMetaForce energy (ReferenceATMMetaForceKernels.cpp:98) */
+#define ATM_RES_PERT 1        /* soft-cored perturbation energy usc (:86) */
+#define ATM_RES_SP 2          /* dW/du (:101) */
+#define ATM_RES_W 3           /* softplus bias energy W (:89-94) */
+#define ATM_RES_U 4           /* raw u = U2-U1 (dir>0) or U1-U2 (:84) */
+#define ATM_RES_E0 5          /* U1 (dir>0) or U2 (:85) */
+#define ATM_RES_BFP 6         /* dW/dusc (:95) */
+#define ATM_RES_FP 7          /* dusc/du (:35) */
+#define ATM_RES_E1 8          /* U_var at x */
+#define ATM_RES_E2 9          /* U_var at x + d */
+#define ATM_RES_DW_DLAMBDA1 10
+#define ATM_RES_DW_DLAMBDA2 11
+#define ATM_RES_DW_DALPHA 12
+#define ATM_RES_DW_DU0 13
+#define ATM_RES_DW_DW0 14
+#define ATM_RES_STATUS 15     /* device status word (0 = ok) */
+#define ATM_NUM_RES 16
+
+typedef struct atm_force_s* atm_force_t;
+typedef struct atm_nonbonded_s* atm_nonbonded_t;
+typedef struct atm_system_s* atm_system_t;
+typedef struct atm_context_s* atm_context_t;
+typedef struct atm_batch_s* atm_batch_t;
+
+/* Message of the last failure on this thread ("" if none). */
+const char* atm_last_error(void);
+/* ATMMetaForce::Version(), ATMMetaForce.h:223-227 / ATMMetaForceVersion.h:4. */
+const char* atm_version(void);
+/* ATMMetaForce::Lambda1() ... Direction(), ATMMetaForce.h:151-218; which = ATM_LAMBDA1..ATM_DIRECTION. */
+const char* atm_global_name(int which);
+
+/* ---- ATMMetaForce (ATMMetaForce.h:54-315, ATMMetaForce.cpp:12-44) --------- */
+/* Constructor, ATMMetaForce.h:79-83. */
+int atm_force_create(double lambda1, double lambda2, double alpha, double u0, double w0, double umax,
+                     double ubcore, double acore, double direction, const int* variable_groups, int n_groups,
+                     atm_force_t* out);
+/* Frees a force that was never added to a system (a system owns its forces). */
+int atm_force_destroy(atm_force_t force);
+/* addParticle, ATMMetaForce.h:104 / ATMMetaForce.cpp:12-15. */
+int atm_force_add_particle(atm_force_t force, int particle, double dx, double dy, double dz, int* index);
+/* getParticleParameters, ATMMetaForce.h:113 / ATMMetaForce.cpp:17-24. */
+int atm_force_get_particle_parameters(atm_force_t force, int index, int* particle, double* dx, double* dy, double* dz);
+/* setParticleParameters, ATMMetaForce.h:122 / ATMMetaForce.cpp:26-32. */
+int atm_force_set_particle_parameters(atm_force_t force, int index, int particle, double dx, double dy, double dz);
+/* getNumParticles, ATMMetaForce.h:90-92. */
+int atm_force_get_num_particles(atm_force_t force, int* n);
+/* getDefaultLambda1() ... getDefaultDirection(), ATMMetaForce.h:232-290; which = ATM_LAMBDA1.. */
+int atm_force_get_default(atm_force_t force, int which, double* value);
+/* getVariableForceGroups, ATMMetaForce.h:295-297: writes min(cap, n) groups, n to *n. */
+int atm_force_get_variable_force_groups(atm_force_t force, int* groups, int cap, int* n);
+/* Force::setForceGroup / getForceGroup / setName / getName (OpenMM base class). */
+int atm_force_set_force_group(atm_force_t force, int group);
+int atm_force_get_force_group(atm_force_t force, int* group);
+int atm_force_set_name(atm_force_t force, const char* name);
+int atm_force_get_name(atm_force_t force, char* buf, size_t cap, size_t* len);
+/* usesPeriodicBoundaryConditions, ATMMetaForce.h:135-137 (always 0). */
+int atm_force_uses_periodic_boundary_conditions(atm_force_t force, int* uses);
+/* updateParametersInContext, ATMMetaForce.h:130 / CommonATMMetaForceKernels.cpp:229-251. */
+int atm_force_update_parameters_in_context(atm_force_t force, atm_context_t context);
+/* getPerturbationEnergy, ATMMetaForce.h:145 / ATMMetaForceImpl.cpp:125. */
+int atm_force_get_perturbation_energy(atm_force_t force, atm_context_t context, double* value);
+/* XmlSerializer::serialize<ATMMetaForce> through ATMMetaForceProxy::serialize,
+ * serialization/src/ATMMetaForceProxy.cpp:11-40.  Writes a NUL-terminated
+ * document of at most cap bytes; *len = bytes needed (excluding NUL). */
+int atm_force_serialize(atm_force_t force, char* buf, size_t cap, size_t* len);
+/* ATMMetaForceProxy::deserialize, ATMMetaForceProxy.cpp:42-79. */
+int atm_force_deserialize(const char* xml, atm_force_t* out);
+
+/* ---- inner NonbondedForce (OpenMM NonbondedForce, cloned by ATMMetaForceImpl.cpp:103-108) -- */
+int atm_nonbonded_create(atm_nonbonded_t* out);
+int atm_nonbonded_destroy(atm_nonbonded_t nb);
+int atm_nonbonded_add_particle(atm_nonbonded_t nb, double charge, double sigma, double epsilon, int* index);
+int atm_nonbonded_set_particle_parameters(atm_nonbonded_t nb, int index, double charge, double sigma, double epsilon);
+int atm_nonbonded_get_particle_parameters(atm_nonbonded_t nb, int index, double* charge, double* sigma, double* epsilon);
+int atm_nonbonded_get_num_particles(atm_nonbonded_t nb, int* n);
+/* An exception replaces the pair's interaction (chargeProd 0 and epsilon 0 = exclusion). */
+int atm_nonbonded_add_exception(atm_nonbonded_t nb, int i, int j, double charge_prod, double sigma, double epsilon,
+                                int* index);
+int atm_nonbonded_get_num_exceptions(atm_nonbonded_t nb, int* n);
+int atm_nonbonded_set_method(atm_nonbonded_t nb, int method);
+int atm_nonbonded_set_cutoff(atm_nonbonded_t nb, double cutoff);
+int atm_nonbonded_set_reaction_field_dielectric(atm_nonbonded_t nb, double eps_rf);
+int atm_nonbonded_set_ewald_error_tolerance(atm_nonbonded_t nb, double tol);
+/* alpha = 0 selects OpenMM's rule from the tolerance and the system's default box. */
+int atm_nonbonded_set_pme_parameters(atm_nonbonded_t nb, double alpha, int nx, int ny, int nz);
+int atm_nonbonded_set_use_dispersion_correction(atm_nonbonded_t nb, int use);
+int atm_nonbonded_set_force_group(atm_nonbonded_t nb, int group);
+int atm_nonbonded_get_force_group(atm_nonbonded_t nb, int* group);
+
+/* ---- System --------------------------------------------------------------- */
+int atm_system_create(atm_system_t* out);
+int atm_system_destroy(atm_system_t sys);
+int atm_system_add_particle(atm_system_t sys, double mass, int* index);
+int atm_system_get_num_particles(atm_system_t sys, int* n);
+/* Orthorhombic boxes: a = (ax,0,0), b = (0,by,0), c = (0,0,cz). */
+int atm_system_set_default_periodic_box_vectors(atm_system_t sys, const double* a, const double* b, const double* c);
+/* System::addForce: the system takes ownership of the force object. */
+int atm_system_add_nonbonded(atm_system_t sys, atm_nonbonded_t nb);
+int atm_system_add_atm_force(atm_system_t sys, atm_force_t force);
+
+/* ---- Context: one replica on one GPU -------------------------------------- */
+/* properties: "key=value;key=value".  Keys: DifferencePath=0|1 (default 0, two
+ * full inner evaluations as in ATMMetaForceImpl.cpp:113,116). */
+int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out);
+int atm_context_destroy(atm_context_t ctx);
+/* Context::setPositions (host doubles, n x 3, nm). */
+int atm_context_set_positions(atm_context_t ctx, const double* pos, int n);
+int atm_context_set_periodic_box_vectors(atm_context_t ctx, const double* a, const double* b, const double* c);
+/* Context::setParameter / getParameter for the ATM globals (ATMMetaForceImpl.cpp:175-187). */
+int atm_context_set_parameter(atm_context_t ctx, const char* name, double value);
+int atm_context_get_parameter(atm_context_t ctx, const char* name, double* value);
+/* Context::getState(getEnergy, getForces, groups): energy and forces (n x 3,
+ * host, nullable) of the forces whose group bit is set in groups_mask
+ * (ATMMetaForceImpl.cpp:135-173: the ATM force contributes only when its group
+ * is requested; its forces are merged even if forces are not requested). */
+int atm_context_get_state(atm_context_t ctx, int groups_mask, double* energy, double* forces);
+/* Last per-replica result record (ATM_NUM_RES doubles). */
+int atm_context_get_results(atm_context_t ctx, double* results);
+
+/* ---- Batch: R replicas in one CUDA graph ----------------------------------- */
+/* systems[r] each hold one NonbondedForce and one ATMMetaForce (copied; the
+ * systems stay owned by the caller).  properties as for contexts
+ * (DifferencePath defaults to 1 here). */
+int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
+                     atm_batch_t* out);
+int atm_batch_destroy(atm_batch_t b);
+int atm_batch_get_num_replicas(atm_batch_t b, int* r);
+int atm_batch_get_num_particles(atm_batch_t b, int replica, int* n);
+int atm_batch_set_positions(atm_batch_t b, int replica, const double* pos);
+int atm_batch_set_parameter(atm_batch_t b, int replica, const char* name, double value);
+int atm_batch_set_periodic_box_vectors(atm_batch_t b, int replica, const double* a, const double* b_, const double* c);
+/* One evaluation of every replica.  pos_all (nullable: keep the stored
+ * positions) holds the replicas' positions back to back (host, nm); energies
+ * (R), forces (sum n_r x 3, host) and results (R x ATM_NUM_RES) are nullable. */
+int atm_batch_evaluate(atm_batch_t b, const double* pos_all, double* energies, double* forces, double* results);
+/* Same with device pointers on the caller's CUDA stream (cudaStream_t as void*). */
+int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_forces, double* d_results,
+                              void* stream);
+/* R x R matrix of beta * (e0_r + W_s(u_r)): replica r's coordinates under
+ * replica s's alchemical parameters, from the last evaluation. */
+int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix);
+
+/* ---- diagnostics ------------------------------------------------------------ */
+/* Timings (ms) of the kernels of the last evaluate() when profiling is on. */
+int atm_batch_set_profiling(atm_batch_t b, int on);
+int atm_batch_get_kernel_times(atm_batch_t b, char* names, size_t names_cap, double* ms, int cap, int* n);
+/* Number of the library's own kernel launches per evaluation. */
+int atm_batch_get_launch_count(atm_batch_t b, int* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,694 @@
+// extern "C" entry points of include/atm_capi.h.
+//
+// Every entry point converts C++ exceptions into ATM_* status codes and a
+// thread-local message, the way the reference's SWIG layer turns C++
+// exceptions into Python exceptions (python/atmmetaforceplugin.i:54-61).
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/atm_capi.h"
+#include "engine.h"
+#include "model.h"
+
+using namespace atm;
+
+struct atm_force_s {
+    std::unique_ptr<ATMMetaForce> f;
+    bool owned_by_system = false;
+};
+struct atm_nonbonded_s {
+    std::unique_ptr<NonbondedForce> nb;
+    bool owned_by_system = false;
+};
+struct atm_system_s {
+    System sys;
+    atm_force_t atm_handle = nullptr;
+    atm_nonbonded_t nb_handle = nullptr;
+};
+
+struct atm_context_s {
+    std::unique_ptr<Engine> eng;
+    int atm_group = 0, nb_group = 0;
+    bool var_nb = true;
+    int n = 0;
+    std::vector<int> particle_ids;  // ATMMetaForce particle field at creation
+    bool positions_set = false;
+    bool dirty = true;
+    double pert = 0.0;
+    std::vector<double> forces, forces_nb;
+    std::vector<double> results;
+};
+
+struct atm_batch_s {
+    std::unique_ptr<Engine> eng;
+    std::vector<double> results;
+    std::vector<double> matrix;
+    bool evaluated = false;
+};
+
+static thread_local std::string g_error;
+
+#define API_BEGIN try {
+#define API_END                                    \
+    g_error.clear();                               \
+    return ATM_OK;                                 \
+    }                                              \
+    catch (const Error& e) {                       \
+        g_error = e.what();                        \
+        return e.code;                             \
+    }                                              \
+    catch (const std::exception& e) {              \
+        g_error = e.what();                        \
+        return ATM_ERR_INVALID_ARGUMENT;           \
+    }                                              \
+    catch (...) {                                  \
+        g_error = "unknown error";                 \
+        return ATM_ERR_INVALID_ARGUMENT;           \
+    }
+
+#define REQUIRE(cond, code, msg) \
+    if (!(cond)) throw Error(code, msg)
+
+static std::map<std::string, std::string> parse_props(const char* p) {
+    std::map<std::string, std::string> m;
+    if (!p) return m;
+    std::stringstream ss(p);
+    std::string item;
+    while (std::getline(ss, item, ';')) {
+        auto eq = item.find('=');
+        if (eq == std::string::npos) continue;
+        m[item.substr(0, eq)] = item.substr(eq + 1);
+    }
+    return m;
+}
+
+static bool prop_bool(const std::map<std::string, std::string>& m, const char* key, bool def) {
+    auto it = m.find(key);
+    if (it == m.end()) return def;
+    const std::string& v = it->second;
+    if (v == "1" || v == "true" || v == "True") return true;
+    if (v == "0" || v == "false" || v == "False") return false;
+    throw Error(ATM_ERR_INVALID_ARGUMENT, std::string("Bad value for property ") + key + ": " + v);
+}
+
+extern "C" {
+
+const char* atm_last_error(void) { return g_error.c_str(); }
+const char* atm_version(void) { return kVersion; }
+const char* atm_global_name(int which) { return global_name(which); }
+
+// ---- ATMMetaForce ---------------------------------------------------------
+
+int atm_force_create(double lambda1, double lambda2, double alpha, double u0, double w0, double umax, double ubcore,
+                     double acore, double direction, const int* groups, int n_groups, atm_force_t* out) {
+    API_BEGIN
+    REQUIRE(out, ATM_ERR_INVALID_ARGUMENT, "null output handle");
+    REQUIRE(n_groups >= 0 && (n_groups == 0 || groups), ATM_ERR_INVALID_ARGUMENT, "bad variable group list");
+    std::vector<int> g(groups, groups + n_groups);
+    auto* h = new atm_force_s;
+    h->f.reset(new ATMMetaForce(lambda1, lambda2, alpha, u0, w0, umax, ubcore, acore, direction, g));
+    *out = h;
+    API_END
+}
+
+int atm_force_destroy(atm_force_t force) {
+    API_BEGIN
+    if (!force) return ATM_OK;
+    REQUIRE(!force->owned_by_system, ATM_ERR_STATE, "the force is owned by a System");
+    delete force;
+    API_END
+}
+
+int atm_force_add_particle(atm_force_t force, int particle, double dx, double dy, double dz, int* index) {
+    API_BEGIN
+    REQUIRE(force, ATM_ERR_INVALID_ARGUMENT, "null force");
+    int k = force->f->addParticle(particle, dx, dy, dz);
+    if (index) *index = k;
+    API_END
+}
+
+int atm_force_get_particle_parameters(atm_force_t force, int index, int* particle, double* dx, double* dy, double* dz) {
+    API_BEGIN
+    REQUIRE(force && particle && dx && dy && dz, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    force->f->getParticleParameters(index, *particle, *dx, *dy, *dz);
+    API_END
+}
+
+int atm_force_set_particle_parameters(atm_force_t force, int index, int particle, double dx, double dy, double dz) {
+    API_BEGIN
+    REQUIRE(force, ATM_ERR_INVALID_ARGUMENT, "null force");
+    force->f->setParticleParameters(index, particle, dx, dy, dz);
+    API_END
+}
+
+int atm_force_get_num_particles(atm_force_t force, int* n) {
+    API_BEGIN
+    REQUIRE(force && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = force->f->getNumParticles();
+    API_END
+}
+
+int atm_force_get_default(atm_force_t force, int which, double* value) {
+    API_BEGIN
+    REQUIRE(force && value, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(which >= 0 && which < NUM_GLOBALS, ATM_ERR_INDEX, "unknown parameter index");
+    *value = force->f->getDefault(which);
+    API_END
+}
+
+int atm_force_get_variable_force_groups(atm_force_t force, int* groups, int cap, int* n) {
+    API_BEGIN
+    REQUIRE(force && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    const auto& g = force->f->getVariableForceGroups();
+    *n = (int)g.size();
+    for (int k = 0; k < (int)g.size() && k < cap; k++) groups[k] = g[k];
+    API_END
+}
+
+int atm_force_set_force_group(atm_force_t force, int group) {
+    API_BEGIN
+    REQUIRE(force, ATM_ERR_INVALID_ARGUMENT, "null force");
+    force->f->setForceGroup(group);
+    API_END
+}
+
+int atm_force_get_force_group(atm_force_t force, int* group) {
+    API_BEGIN
+    REQUIRE(force && group, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *group = force->f->getForceGroup();
+    API_END
+}
+
+int atm_force_set_name(atm_force_t force, const char* name) {
+    API_BEGIN
+    REQUIRE(force && name, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    force->f->setName(name);
+    API_END
+}
+
+static void copy_string(const std::string& s, char* buf, size_t cap, size_t* len) {
+    if (len) *len = s.size();
+    if (buf && cap > 0) {
+        size_t k = s.size() < cap - 1 ? s.size() : cap - 1;
+        std::memcpy(buf, s.data(), k);
+        buf[k] = '\0';
+    }
+}
+
+int atm_force_get_name(atm_force_t force, char* buf, size_t cap, size_t* len) {
+    API_BEGIN
+    REQUIRE(force, ATM_ERR_INVALID_ARGUMENT, "null force");
+    copy_string(force->f->getName(), buf, cap, len);
+    API_END
+}
+
+int atm_force_uses_periodic_boundary_conditions(atm_force_t force, int* uses) {
+    API_BEGIN
+    REQUIRE(force && uses, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *uses = 0;  // ATMMetaForce.h:135-137
+    API_END
+}
+
+int atm_force_update_parameters_in_context(atm_force_t force, atm_context_t ctx) {
+    API_BEGIN
+    REQUIRE(force && ctx, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    const ATMMetaForce& f = *force->f;
+    // ReferenceATMMetaForceKernels.cpp:146-154: the particle count and indices may not change
+    REQUIRE(f.getNumParticles() == ctx->n, ATM_ERR_PARTICLES,
+            "copyParametersToContext: The number of ATMMetaForce particles has changed");
+    std::vector<double> d(3 * (size_t)ctx->n);
+    for (int i = 0; i < ctx->n; i++) {
+        REQUIRE(f.particles[i].particle == ctx->particle_ids[i], ATM_ERR_PARTICLES,
+                "copyParametersToContext: A particle index has changed");
+        d[3 * i] = f.particles[i].dx;
+        d[3 * i + 1] = f.particles[i].dy;
+        d[3 * i + 2] = f.particles[i].dz;
+    }
+    ctx->eng->set_displacements(0, d.data());
+    ctx->dirty = true;
+    API_END
+}
+
+int atm_force_get_perturbation_energy(atm_force_t force, atm_context_t ctx, double* value) {
+    API_BEGIN
+    REQUIRE(force && ctx && value, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *value = ctx->pert;
+    API_END
+}
+
+int atm_force_serialize(atm_force_t force, char* buf, size_t cap, size_t* len) {
+    API_BEGIN
+    REQUIRE(force, ATM_ERR_INVALID_ARGUMENT, "null force");
+    copy_string(serialize(*force->f), buf, cap, len);
+    API_END
+}
+
+int atm_force_deserialize(const char* xml, atm_force_t* out) {
+    API_BEGIN
+    REQUIRE(xml && out, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    auto f = deserialize(xml);
+    auto* h = new atm_force_s;
+    h->f = std::move(f);
+    *out = h;
+    API_END
+}
+
+// ---- NonbondedForce -------------------------------------------------------
+
+int atm_nonbonded_create(atm_nonbonded_t* out) {
+    API_BEGIN
+    REQUIRE(out, ATM_ERR_INVALID_ARGUMENT, "null output handle");
+    auto* h = new atm_nonbonded_s;
+    h->nb.reset(new NonbondedForce);
+    *out = h;
+    API_END
+}
+
+int atm_nonbonded_destroy(atm_nonbonded_t nb) {
+    API_BEGIN
+    if (!nb) return ATM_OK;
+    REQUIRE(!nb->owned_by_system, ATM_ERR_STATE, "the force is owned by a System");
+    delete nb;
+    API_END
+}
+
+int atm_nonbonded_add_particle(atm_nonbonded_t nb, double charge, double sigma, double epsilon, int* index) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    int k = nb->nb->addParticle(charge, sigma, epsilon);
+    if (index) *index = k;
+    API_END
+}
+
+int atm_nonbonded_set_particle_parameters(atm_nonbonded_t nb, int index, double charge, double sigma, double epsilon) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(index >= 0 && index < (int)nb->nb->charge.size(), ATM_ERR_INDEX, "Index out of range");
+    nb->nb->charge[index] = charge;
+    nb->nb->sigma[index] = sigma;
+    nb->nb->epsilon[index] = epsilon;
+    API_END
+}
+
+int atm_nonbonded_get_particle_parameters(atm_nonbonded_t nb, int index, double* charge, double* sigma,
+                                          double* epsilon) {
+    API_BEGIN
+    REQUIRE(nb && charge && sigma && epsilon, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(index >= 0 && index < (int)nb->nb->charge.size(), ATM_ERR_INDEX, "Index out of range");
+    *charge = nb->nb->charge[index];
+    *sigma = nb->nb->sigma[index];
+    *epsilon = nb->nb->epsilon[index];
+    API_END
+}
+
+int atm_nonbonded_get_num_particles(atm_nonbonded_t nb, int* n) {
+    API_BEGIN
+    REQUIRE(nb && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = (int)nb->nb->charge.size();
+    API_END
+}
+
+int atm_nonbonded_add_exception(atm_nonbonded_t nb, int i, int j, double charge_prod, double sigma, double epsilon,
+                                int* index) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(i >= 0 && j >= 0, ATM_ERR_INDEX, "Index out of range");
+    int k = nb->nb->addException(i, j, charge_prod, sigma, epsilon);
+    if (index) *index = k;
+    API_END
+}
+
+int atm_nonbonded_get_num_exceptions(atm_nonbonded_t nb, int* n) {
+    API_BEGIN
+    REQUIRE(nb && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = (int)nb->nb->exceptions.size();
+    API_END
+}
+
+int atm_nonbonded_set_method(atm_nonbonded_t nb, int method) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(method == 0 || method == 1 || method == 2 || method == 4, ATM_ERR_UNSUPPORTED,
+            "Unsupported nonbonded method");
+    nb->nb->method = method;
+    API_END
+}
+
+int atm_nonbonded_set_cutoff(atm_nonbonded_t nb, double cutoff) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(cutoff > 0, ATM_ERR_INVALID_ARGUMENT, "The cutoff must be positive");
+    nb->nb->cutoff = cutoff;
+    API_END
+}
+
+int atm_nonbonded_set_reaction_field_dielectric(atm_nonbonded_t nb, double eps_rf) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    nb->nb->epsRF = eps_rf;
+    API_END
+}
+
+int atm_nonbonded_set_ewald_error_tolerance(atm_nonbonded_t nb, double tol) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(tol > 0 && tol < 0.5, ATM_ERR_INVALID_ARGUMENT, "Bad Ewald error tolerance");
+    nb->nb->ewaldTol = tol;
+    API_END
+}
+
+int atm_nonbonded_set_pme_parameters(atm_nonbonded_t nb, double alpha, int nx, int ny, int nz) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    nb->nb->alpha = alpha;
+    nb->nb->grid[0] = nx;
+    nb->nb->grid[1] = ny;
+    nb->nb->grid[2] = nz;
+    API_END
+}
+
+int atm_nonbonded_set_use_dispersion_correction(atm_nonbonded_t nb, int use) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    nb->nb->dispersionCorrection = use != 0;
+    API_END
+}
+
+int atm_nonbonded_set_force_group(atm_nonbonded_t nb, int group) {
+    API_BEGIN
+    REQUIRE(nb, ATM_ERR_INVALID_ARGUMENT, "null force");
+    REQUIRE(group >= 0 && group <= 31, ATM_ERR_INVALID_ARGUMENT, "Force group must be between 0 and 31");
+    nb->nb->forceGroup = group;
+    API_END
+}
+
+int atm_nonbonded_get_force_group(atm_nonbonded_t nb, int* group) {
+    API_BEGIN
+    REQUIRE(nb && group, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *group = nb->nb->forceGroup;
+    API_END
+}
+
+// ---- System ---------------------------------------------------------------
+
+int atm_system_create(atm_system_t* out) {
+    API_BEGIN
+    REQUIRE(out, ATM_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = new atm_system_s;
+    API_END
+}
+
+int atm_system_destroy(atm_system_t sys) {
+    API_BEGIN
+    if (!sys) return ATM_OK;
+    if (sys->atm_handle) {
+        sys->atm_handle->f.release();  // the System's unique_ptr owns the object
+        delete sys->atm_handle;
+    }
+    if (sys->nb_handle) {
+        sys->nb_handle->nb.release();
+        delete sys->nb_handle;
+    }
+    delete sys;
+    API_END
+}
+
+int atm_system_add_particle(atm_system_t sys, double mass, int* index) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    int k = sys->sys.addParticle(mass);
+    if (index) *index = k;
+    API_END
+}
+
+int atm_system_get_num_particles(atm_system_t sys, int* n) {
+    API_BEGIN
+    REQUIRE(sys && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = (int)sys->sys.masses.size();
+    API_END
+}
+
+static void read_box(const double* a, const double* b, const double* c, double* box) {
+    REQUIRE(a && b && c, ATM_ERR_INVALID_ARGUMENT, "null box vector");
+    REQUIRE(a[1] == 0 && a[2] == 0 && b[0] == 0 && b[2] == 0 && c[0] == 0 && c[1] == 0, ATM_ERR_UNSUPPORTED,
+            "Only rectangular periodic boxes are supported");
+    REQUIRE(a[0] > 0 && b[1] > 0 && c[2] > 0, ATM_ERR_INVALID_ARGUMENT, "Box vectors must be positive");
+    box[0] = a[0];
+    box[1] = b[1];
+    box[2] = c[2];
+}
+
+int atm_system_set_default_periodic_box_vectors(atm_system_t sys, const double* a, const double* b, const double* c) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    read_box(a, b, c, sys->sys.box);
+    API_END
+}
+
+int atm_system_add_nonbonded(atm_system_t sys, atm_nonbonded_t nb) {
+    API_BEGIN
+    REQUIRE(sys && nb, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(!nb->owned_by_system, ATM_ERR_STATE, "The force already belongs to a System");
+    REQUIRE(!sys->sys.nonbonded, ATM_ERR_UNSUPPORTED, "Only one NonbondedForce per System is supported");
+    sys->sys.nonbonded.reset(nb->nb.get());
+    nb->owned_by_system = true;
+    sys->nb_handle = nb;
+    API_END
+}
+
+int atm_system_add_atm_force(atm_system_t sys, atm_force_t force) {
+    API_BEGIN
+    REQUIRE(sys && force, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(!force->owned_by_system, ATM_ERR_STATE, "The force already belongs to a System");
+    REQUIRE(!sys->sys.atm, ATM_ERR_UNSUPPORTED, "Only one ATMMetaForce per System is supported");
+    sys->sys.atm.reset(force->f.get());
+    force->owned_by_system = true;
+    sys->atm_handle = force;
+    API_END
+}
+
+// ---- Context --------------------------------------------------------------
+
+int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out) {
+    API_BEGIN
+    REQUIRE(sys && out, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    auto props = parse_props(properties);
+    bool diff = prop_bool(props, "DifferencePath", false);
+    ReplicaSpec spec = spec_from_system(sys->sys);
+    std::unique_ptr<atm_context_s> c(new atm_context_s);
+    c->atm_group = sys->sys.atm->getForceGroup();
+    c->nb_group = sys->sys.nonbonded->forceGroup;
+    c->var_nb = spec.var_nb;
+    c->n = spec.n;
+    for (const auto& p : sys->sys.atm->particles) c->particle_ids.push_back(p.particle);
+    std::vector<ReplicaSpec> v;
+    v.push_back(std::move(spec));
+    c->eng.reset(new Engine(std::move(v), device, !diff));
+    c->forces.resize(3 * (size_t)c->n);
+    c->forces_nb.resize(3 * (size_t)c->n);
+    c->results.resize(NUM_RES);
+    *out = c.release();
+    API_END
+}
+
+int atm_context_destroy(atm_context_t ctx) {
+    API_BEGIN
+    delete ctx;
+    API_END
+}
+
+int atm_context_set_positions(atm_context_t ctx, const double* pos, int n) {
+    API_BEGIN
+    REQUIRE(ctx && pos, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(n == ctx->n, ATM_ERR_INVALID_ARGUMENT, "Called setPositions() on a Context with the wrong number of positions");
+    ctx->eng->set_positions(0, pos);
+    ctx->positions_set = true;
+    ctx->dirty = true;
+    API_END
+}
+
+int atm_context_set_periodic_box_vectors(atm_context_t ctx, const double* a, const double* b, const double* c) {
+    API_BEGIN
+    REQUIRE(ctx, ATM_ERR_INVALID_ARGUMENT, "null context");
+    double box[3];
+    read_box(a, b, c, box);
+    ctx->eng->set_box(0, box);
+    ctx->dirty = true;
+    API_END
+}
+
+int atm_context_set_parameter(atm_context_t ctx, const char* name, double value) {
+    API_BEGIN
+    REQUIRE(ctx && name, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    int k = global_index(name);
+    REQUIRE(k >= 0, ATM_ERR_INVALID_ARGUMENT, std::string("Called setParameter() with invalid parameter name: ") + name);
+    ctx->eng->set_param(0, k, value);
+    ctx->dirty = true;
+    API_END
+}
+
+int atm_context_get_parameter(atm_context_t ctx, const char* name, double* value) {
+    API_BEGIN
+    REQUIRE(ctx && name && value, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    int k = global_index(name);
+    REQUIRE(k >= 0, ATM_ERR_INVALID_ARGUMENT, std::string("Called getParameter() with invalid parameter name: ") + name);
+    *value = ctx->eng->param(0, k);
+    API_END
+}
+
+int atm_context_get_state(atm_context_t ctx, int groups_mask, double* energy, double* forces) {
+    API_BEGIN
+    REQUIRE(ctx, ATM_ERR_INVALID_ARGUMENT, "null context");
+    REQUIRE(ctx->positions_set, ATM_ERR_STATE, "Particle positions have not been set");
+    bool want_atm = (groups_mask >> ctx->atm_group) & 1;
+    bool want_nb = (groups_mask >> ctx->nb_group) & 1;
+    if ((want_atm || want_nb) && ctx->dirty) {
+        ctx->eng->evaluate(nullptr, ctx->forces.data(), ctx->forces_nb.data(), ctx->results.data(), nullptr);
+        ctx->dirty = false;
+    }
+    // ATMMetaForceImpl.cpp:148,169-172: the perturbation energy is refreshed when the ATM group is evaluated
+    if (want_atm) ctx->pert = ctx->results[RES_PERT];
+    double e = 0.0;
+    if (want_atm) e += ctx->results[RES_ENERGY];
+    if (want_nb) e += ctx->results[RES_E1];
+    if (energy) *energy = e;
+    if (forces) {
+        for (size_t k = 0; k < ctx->forces.size(); k++)
+            forces[k] = (want_atm ? ctx->forces[k] : 0.0) + (want_nb ? ctx->forces_nb[k] : 0.0);
+    }
+    API_END
+}
+
+int atm_context_get_results(atm_context_t ctx, double* results) {
+    API_BEGIN
+    REQUIRE(ctx && results, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    std::memcpy(results, ctx->results.data(), sizeof(double) * NUM_RES);
+    API_END
+}
+
+// ---- Batch ----------------------------------------------------------------
+
+int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
+                     atm_batch_t* out) {
+    API_BEGIN
+    REQUIRE(systems && out && n_replicas > 0, ATM_ERR_INVALID_ARGUMENT, "bad argument");
+    auto props = parse_props(properties);
+    bool diff = prop_bool(props, "DifferencePath", true);
+    std::vector<ReplicaSpec> v;
+    for (int r = 0; r < n_replicas; r++) {
+        REQUIRE(systems[r], ATM_ERR_INVALID_ARGUMENT, "null system");
+        v.push_back(spec_from_system(systems[r]->sys));
+    }
+    std::unique_ptr<atm_batch_s> b(new atm_batch_s);
+    b->eng.reset(new Engine(std::move(v), device, !diff));
+    b->results.resize((size_t)NUM_RES * n_replicas);
+    b->matrix.resize((size_t)n_replicas * n_replicas);
+    *out = b.release();
+    API_END
+}
+
+int atm_batch_destroy(atm_batch_t b) {
+    API_BEGIN
+    delete b;
+    API_END
+}
+
+int atm_batch_get_num_replicas(atm_batch_t b, int* r) {
+    API_BEGIN
+    REQUIRE(b && r, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *r = b->eng->replicas();
+    API_END
+}
+
+int atm_batch_get_num_particles(atm_batch_t b, int replica, int* n) {
+    API_BEGIN
+    REQUIRE(b && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(replica >= 0 && replica < b->eng->replicas(), ATM_ERR_INDEX, "Replica index out of range");
+    *n = b->eng->atoms(replica);
+    API_END
+}
+
+int atm_batch_set_positions(atm_batch_t b, int replica, const double* pos) {
+    API_BEGIN
+    REQUIRE(b && pos, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    b->eng->set_positions(replica, pos);
+    API_END
+}
+
+int atm_batch_set_parameter(atm_batch_t b, int replica, const char* name, double value) {
+    API_BEGIN
+    REQUIRE(b && name, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    int k = global_index(name);
+    REQUIRE(k >= 0, ATM_ERR_INVALID_ARGUMENT, std::string("Called setParameter() with invalid parameter name: ") + name);
+    b->eng->set_param(replica, k, value);
+    API_END
+}
+
+int atm_batch_set_periodic_box_vectors(atm_batch_t b, int replica, const double* a, const double* b_, const double* c) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    double box[3];
+    read_box(a, b_, c, box);
+    b->eng->set_box(replica, box);
+    API_END
+}
+
+int atm_batch_evaluate(atm_batch_t b, const double* pos_all, double* energies, double* forces, double* results) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    if (pos_all) b->eng->set_all_positions(pos_all);
+    b->eng->evaluate(energies, forces, nullptr, b->results.data(), b->matrix.data());
+    if (results) std::memcpy(results, b->results.data(), sizeof(double) * b->results.size());
+    b->evaluated = true;
+    API_END
+}
+
+int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_forces, double* d_results,
+                              void* stream) {
+    API_BEGIN
+    REQUIRE(b && d_pos_all, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    b->eng->evaluate_device(d_pos_all, d_forces, d_results, (cudaStream_t)stream);
+    API_END
+}
+
+int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix) {
+    API_BEGIN
+    REQUIRE(b && matrix, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(b->evaluated, ATM_ERR_STATE, "No evaluation has been run");
+    for (size_t k = 0; k < b->matrix.size(); k++) matrix[k] = beta * b->matrix[k];
+    API_END
+}
+
+int atm_batch_set_profiling(atm_batch_t b, int on) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    b->eng->set_profiling(on != 0);
+    API_END
+}
+
+int atm_batch_get_kernel_times(atm_batch_t b, char* names, size_t names_cap, double* ms, int cap, int* n) {
+    API_BEGIN
+    REQUIRE(b && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    const auto& t = b->eng->kernel_times();
+    *n = (int)t.size();
+    std::string joined;
+    for (size_t k = 0; k < t.size(); k++) {
+        if (k) joined += ",";
+        joined += t[k].name;
+        if (ms && (int)k < cap) ms[k] = t[k].ms;
+    }
+    copy_string(joined, names, names_cap, nullptr);
+    API_END
+}
+
+int atm_batch_get_launch_count(atm_batch_t b, int* n) {
+    API_BEGIN
+    REQUIRE(b && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = b->eng->launches_per_eval();
+    API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,946 @@
+// Host side of the GPU evaluation engine: atom layout, buffers, cuFFT plans and
+// the CUDA graph that runs one ATM evaluation of all replicas.
+//
+// Reference correspondence: the engine replaces ATMMetaForceImpl's two linked
+// inner contexts (ATMMetaForceImpl.cpp:135-173) and CommonCalcATMMetaForceKernel
+// (CommonATMMetaForceKernels.cpp:78-251): CopyState becomes the displacement of
+// the state-2 slots (k_prepare), the two inner evaluations become one pass over
+// both states (or over state 1 plus the ligand difference), and execute() runs
+// on the device in FP64 with no host round trip for E1/E2.
+#include "engine.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <set>
+#include <sstream>
+#include <unordered_set>
+
+namespace atm {
+
+#define CUDA_CHECK(x)                                                                                   \
+    do {                                                                                                \
+        cudaError_t err__ = (x);                                                                        \
+        if (err__ != cudaSuccess)                                                                       \
+            throw Error(4, std::string("CUDA error: ") + cudaGetErrorString(err__) + " at " #x);        \
+    } while (0)
+#define CUFFT_CHECK(x)                                                                                  \
+    do {                                                                                                \
+        cufftResult r__ = (x);                                                                          \
+        if (r__ != CUFFT_SUCCESS) throw Error(4, std::string("cuFFT error ") + std::to_string((int)r__)); \
+    } while (0)
+
+static const double kOne4PiEps0 = 138.935456;  // kJ mol^-1 nm e^-2 (OpenMM 7.x)
+static const double kPi = 3.14159265358979323846;
+
+ReplicaSpec spec_from_system(const System& sys) {
+    if (!sys.nonbonded) throw Error(5, "The system has no NonbondedForce");
+    if (!sys.atm) throw Error(5, "The system has no ATMMetaForce");
+    const NonbondedForce& nb = *sys.nonbonded;
+    const ATMMetaForce& f = *sys.atm;
+    int n = (int)sys.masses.size();
+    if ((int)nb.charge.size() != n) throw Error(1, "NonbondedForce particle count differs from the System's");
+    if (f.getNumParticles() != n)
+        throw Error(9, "ATMMetaForce must hold every System particle (ATMMetaForce.h:94-104)");
+    // ATMMetaForceImpl.cpp:120-126
+    for (int g : f.groups) {
+        if (g == f.forceGroup) throw Error(8, "The ATM Meta Force group cannot be one of the variable force groups.");
+        if (g < 0 || g > 31) throw Error(1, "Variable force groups must be between 0 and 31");
+    }
+    ReplicaSpec s;
+    s.n = n;
+    s.q = nb.charge;
+    s.sig = nb.sigma;
+    s.eps = nb.epsilon;
+    s.exc = nb.exceptions;
+    s.displ.resize(3 * (size_t)n);
+    // displacement indexed by the force's particle index (ReferenceATMMetaForceKernels.cpp:121-123)
+    for (int i = 0; i < n; i++) {
+        s.displ[3 * i] = f.particles[i].dx;
+        s.displ[3 * i + 1] = f.particles[i].dy;
+        s.displ[3 * i + 2] = f.particles[i].dz;
+    }
+    s.method = nb.method;
+    s.cutoff = nb.cutoff;
+    s.epsRF = nb.epsRF;
+    s.dispersion = nb.dispersionCorrection;
+    for (int a = 0; a < 3; a++) s.box[a] = sys.box[a];
+    if (nb.method == NonbondedForce::PME) {
+        if (nb.alpha > 0 && nb.grid[0] > 0 && nb.grid[1] > 0 && nb.grid[2] > 0) {
+            s.alpha = nb.alpha;
+            for (int a = 0; a < 3; a++) s.grid[a] = nb.grid[a];
+        } else {
+            pme_parameters(nb.cutoff, nb.ewaldTol, sys.box, s.alpha, s.grid);
+            if (nb.alpha > 0) s.alpha = nb.alpha;
+        }
+    }
+    for (int k = 0; k < NUM_GLOBALS; k++) s.params[k] = f.defaults[k];
+    s.var_nb = false;
+    for (int g : f.groups)
+        if (g == nb.forceGroup) s.var_nb = true;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// 3D Hilbert index (J. Skilling, "Programming the Hilbert curve", AIP Conf.
+// Proc. 707, 381 (2004): axes -> transposed index, then bit interleave)
+// ---------------------------------------------------------------------------
+static uint64_t hilbert3(uint32_t x, uint32_t y, uint32_t z, int bits) {
+    uint32_t X[3] = {x, y, z};
+    uint32_t M = 1u << (bits - 1);
+    for (uint32_t Q = M; Q > 1; Q >>= 1) {
+        uint32_t P = Q - 1;
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    for (int i = 1; i < 3; i++) X[i] ^= X[i - 1];
+    uint32_t t = 0;
+    for (uint32_t Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    for (int i = 0; i < 3; i++) X[i] ^= t;
+    uint64_t h = 0;
+    for (int b = bits - 1; b >= 0; b--)
+        for (int i = 0; i < 3; i++) h = (h << 1) | ((X[i] >> b) & 1u);
+    return h;
+}
+
+// |sum_{k=0}^{3} M5(k+1) e^{2 pi i m k / K}|^2 with the mean-of-neighbours repair
+static void bspline_moduli(int K, std::vector<double>& mod) {
+    const double c[4] = {1.0 / 24.0, 11.0 / 24.0, 11.0 / 24.0, 1.0 / 24.0};  // M5(1..4)
+    mod.assign(K, 0.0);
+    for (int m = 0; m < K; m++) {
+        double sc = 0, ss = 0;
+        for (int k = 0; k < 4; k++) {
+            double arg = 2.0 * kPi * m * k / K;
+            sc += c[k] * std::cos(arg);
+            ss += c[k] * std::sin(arg);
+        }
+        mod[m] = sc * sc + ss * ss;
+    }
+    std::vector<double> fixed = mod;
+    for (int m = 0; m < K; m++)
+        if (mod[m] < 1e-7) fixed[m] = 0.5 * (mod[(m - 1 + K) % K] + mod[(m + 1) % K]);
+    mod = fixed;
+}
+
+static double dispersion_coefficient(const ReplicaSpec& s) {
+    // 8 pi N^2 (<eps sig^12>/(9 rc^9) - <eps sig^6>/(3 rc^3)), averages over all
+    // particle pairs (self pairs included) grouped by (sigma, epsilon) class
+    std::map<std::pair<double, double>, double> cls;
+    for (int i = 0; i < s.n; i++) cls[{s.sig[i], s.eps[i]}] += 1.0;
+    std::vector<std::pair<std::pair<double, double>, double>> v(cls.begin(), cls.end());
+    double sum1 = 0, sum2 = 0;
+    for (size_t a = 0; a < v.size(); a++)
+        for (size_t b = a; b < v.size(); b++) {
+            double sig = 0.5 * (v[a].first.first + v[b].first.first);
+            double eps = std::sqrt(v[a].first.second * v[b].first.second);
+            double cnt = (a == b) ? v[a].second * (v[a].second + 1) / 2 : v[a].second * v[b].second;
+            double s6 = std::pow(sig, 6.0);
+            sum1 += cnt * eps * s6 * s6;
+            sum2 += cnt * eps * s6;
+        }
+    double N = s.n;
+    double np = N * (N + 1) / 2;
+    sum1 /= np;
+    sum2 /= np;
+    return 8.0 * kPi * N * N * (sum1 / (9.0 * std::pow(s.cutoff, 9)) - sum2 / (3.0 * std::pow(s.cutoff, 3)));
+}
+
+Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode)
+    : R_((int)reps.size()), dev_(device), full_(full_mode), specs_(std::move(reps)) {
+    if (R_ <= 0) throw Error(1, "At least one replica is required");
+    const ReplicaSpec& s0 = specs_[0];
+    method_ = s0.method;
+    cutoff_ = s0.cutoff;
+    if (method_ != NonbondedForce::CutoffPeriodic && method_ != NonbondedForce::PME)
+        throw Error(5, "Only CutoffPeriodic (reaction field) and PME nonbonded methods run on the GPU path");
+    in_off_.resize(R_);
+    for (int r = 0; r < R_; r++) {
+        const ReplicaSpec& s = specs_[r];
+        if (s.n <= 0) throw Error(1, "Empty replica");
+        if (s.method != method_ || s.cutoff != cutoff_ || s.epsRF != s0.epsRF || s.alpha != s0.alpha)
+            throw Error(5, "All replicas of a batch must share the nonbonded method, cutoff and Ewald parameters");
+        for (int a = 0; a < 3; a++)
+            if (!(s.box[a] >= 2.0 * s.cutoff))
+                throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
+        if (s.method == NonbondedForce::PME)
+            for (int a = 0; a < 3; a++)
+                if (s.grid[a] < 6) throw Error(1, "PME grid dimensions must be at least 6");
+        for (const Exception& e : s.exc)
+            if (e.i < 0 || e.j < 0 || e.i >= s.n || e.j >= s.n || e.i == e.j)
+                throw Error(2, "Exception particle index out of range");
+        in_off_[r] = n_in_;
+        n_in_ += s.n;
+    }
+    alpha_ = s0.alpha;
+    double er = s0.epsRF;
+    krf_ = (er - 1.0) / ((2.0 * er + 1.0) * cutoff_ * cutoff_ * cutoff_);
+    crf_ = 3.0 * er / ((2.0 * er + 1.0) * cutoff_);
+
+    CUDA_CHECK(cudaSetDevice(dev_));
+    CUDA_CHECK(cudaStreamCreateWithFlags(&s_main_, cudaStreamNonBlocking));
+    CUDA_CHECK(cudaStreamCreateWithFlags(&s_pme_, cudaStreamNonBlocking));
+    CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+    CUDA_CHECK(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+    CUDA_CHECK(cudaMallocHost(&h_pos_, sizeof(double) * 3 * (size_t)n_in_));
+    CUDA_CHECK(cudaMallocHost(&h_forces_, sizeof(double) * 3 * (size_t)n_in_));
+    CUDA_CHECK(cudaMallocHost(&h_fnb_, sizeof(double) * 3 * (size_t)n_in_));
+    CUDA_CHECK(cudaMallocHost(&h_results_, sizeof(double) * NUM_RES * (size_t)R_));
+    CUDA_CHECK(cudaMallocHost(&h_matrix_, sizeof(double) * (size_t)R_ * R_));
+    CUDA_CHECK(cudaMallocHost(&h_reps_, sizeof(RepDev) * (size_t)R_));
+    CUDA_CHECK(cudaMallocHost(&h_beta_, sizeof(double)));
+    CUDA_CHECK(cudaMallocHost(&h_status_, sizeof(Status)));
+    std::memset(h_pos_, 0, sizeof(double) * 3 * (size_t)n_in_);
+    int sms = 0, per = 0;
+    CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
+    per = tiles_kernel_blocks_per_sm();
+    if (per < 1) per = 1;
+    tile_grid_ = sms * per;
+}
+
+Engine::~Engine() {
+    cudaSetDevice(dev_);
+    if (s_main_) cudaStreamSynchronize(s_main_);
+    destroy_graphs();
+    free_device();
+    for (auto& g : groups_) {
+        if (g.fwd) cufftDestroy(g.fwd);
+        if (g.inv) cufftDestroy(g.inv);
+    }
+    cudaFreeHost(h_pos_);
+    cudaFreeHost(h_forces_);
+    cudaFreeHost(h_fnb_);
+    cudaFreeHost(h_results_);
+    cudaFreeHost(h_matrix_);
+    cudaFreeHost(h_reps_);
+    cudaFreeHost(h_beta_);
+    cudaFreeHost(h_status_);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    if (ev_join_) cudaEventDestroy(ev_join_);
+    if (s_main_) cudaStreamDestroy(s_main_);
+    if (s_pme_) cudaStreamDestroy(s_pme_);
+}
+
+void Engine::destroy_graphs() {
+    if (graph_host_) cudaGraphExecDestroy(graph_host_);
+    if (graph_dev_) cudaGraphExecDestroy(graph_dev_);
+    graph_host_ = graph_dev_ = nullptr;
+}
+
+void Engine::set_positions(int r, const double* pos) {
+    if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
+    std::memcpy(h_pos_ + 3 * (size_t)in_off_[r], pos, sizeof(double) * 3 * (size_t)specs_[r].n);
+}
+
+void Engine::set_all_positions(const double* pos) {
+    std::memcpy(h_pos_, pos, sizeof(double) * 3 * (size_t)n_in_);
+}
+
+void Engine::set_box(int r, const double* box) {
+    if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
+    for (int a = 0; a < 3; a++)
+        if (!(box[a] >= 2.0 * cutoff_))
+            throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
+    for (int a = 0; a < 3; a++) specs_[r].box[a] = box[a];
+}
+
+void Engine::set_param(int r, int which, double v) {
+    if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
+    if (which < 0 || which >= NUM_GLOBALS) throw Error(2, "Unknown global parameter");
+    specs_[r].params[which] = v;
+}
+
+void Engine::set_displacements(int r, const double* displ) {
+    if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
+    ReplicaSpec& s = specs_[r];
+    bool same_classes = true;
+    for (int i = 0; i < s.n && same_classes; i++) {
+        for (int a = 0; a < 3; a++)
+            if (displ[3 * i + a] != s.displ[3 * i + a]) same_classes = false;
+    }
+    if (same_classes) return;
+    std::memcpy(s.displ.data(), displ, sizeof(double) * 3 * (size_t)s.n);
+    // the moving set or its displacement changed: rebuild the layout lazily
+    layout_ready_ = false;
+}
+
+// ---------------------------------------------------------------------------
+// Layout
+// ---------------------------------------------------------------------------
+
+void Engine::build_layout() {
+    orig_.clear();
+    slot_of_.assign(n_in_, -1);
+    block_rep_.clear();
+    block_cls_.clear();
+    qs_.clear();
+    lj_.clear();
+    displ_sorted_.clear();
+    block_d_.clear();
+    masks_.clear();
+    exc_ij_.clear();
+    exc_p_.clear();
+    exc_cta_first_.clear();
+    rep_host_.assign(R_, RepDev{});
+    const double sqk = std::sqrt(kOne4PiEps0);
+
+    std::vector<std::vector<std::pair<int, int>>> blk_ex;  // per block: (J, mask id) J >= I
+    std::vector<std::vector<std::pair<int, int>>> blk_dx;  // per block: cross-class entries
+    int slot = 0;
+    for (int r = 0; r < R_; r++) {
+        const ReplicaSpec& s = specs_[r];
+        RepDev& rd = rep_host_[r];
+        const double* pos = h_pos_ + 3 * (size_t)in_off_[r];
+        // displacement classes, in order of first appearance
+        std::vector<int> cls(s.n, 0);
+        std::vector<std::array<double, 3>> cls_d(1, {0, 0, 0});
+        for (int i = 0; i < s.n; i++) {
+            double dx = s.displ[3 * i], dy = s.displ[3 * i + 1], dz = s.displ[3 * i + 2];
+            if (dx == 0 && dy == 0 && dz == 0) continue;
+            int c = -1;
+            for (size_t k = 1; k < cls_d.size(); k++)
+                if (cls_d[k][0] == dx && cls_d[k][1] == dy && cls_d[k][2] == dz) c = (int)k;
+            if (c < 0) {
+                cls_d.push_back({dx, dy, dz});
+                c = (int)cls_d.size() - 1;
+            }
+            cls[i] = c;
+        }
+        // molecules from the exception graph
+        std::vector<int> parent(s.n);
+        std::iota(parent.begin(), parent.end(), 0);
+        auto find = [&](int x) {
+            while (parent[x] != x) {
+                parent[x] = parent[parent[x]];
+                x = parent[x];
+            }
+            return x;
+        };
+        for (const Exception& e : s.exc) {
+            int a = find(e.i), b = find(e.j);
+            if (a != b) parent[std::max(a, b)] = std::min(a, b);
+        }
+        // non-moving molecules sorted along a Hilbert curve
+        std::map<int, std::vector<int>> mol;
+        for (int i = 0; i < s.n; i++)
+            if (cls[i] == 0) mol[find(i)].push_back(i);
+        std::vector<std::pair<uint64_t, int>> keys;
+        const int bits = 10;
+        for (auto& kv : mol) {
+            int i = kv.second[0];
+            uint32_t c[3];
+            for (int a = 0; a < 3; a++) {
+                double L = s.box[a];
+                double x = pos[3 * i + a] - L * std::floor(pos[3 * i + a] / L);
+                long v = (long)(x / L * (1 << bits));
+                c[a] = (uint32_t)std::min(std::max(v, 0L), (long)(1 << bits) - 1);
+            }
+            keys.push_back({hilbert3(c[0], c[1], c[2], bits), kv.first});
+        }
+        std::sort(keys.begin(), keys.end());
+        std::vector<std::vector<int>> segments(cls_d.size());
+        for (auto& k : keys)
+            for (int i : mol[k.second]) segments[0].push_back(i);
+        for (int i = 0; i < s.n; i++)
+            if (cls[i] != 0) segments[cls[i]].push_back(i);
+
+        rd.slot_begin = slot;
+        rd.block_begin = slot / kTile;
+        rd.mov_block_begin = -1;
+        rd.in_off = in_off_[r];
+        rd.n = s.n;
+        std::vector<int> slot_local(s.n, -1);
+        for (size_t c = 0; c < segments.size(); c++) {
+            if (segments[c].empty()) continue;
+            if (c >= 1 && rd.mov_block_begin < 0) rd.mov_block_begin = slot / kTile;
+            for (int i : segments[c]) {
+                slot_local[i] = slot;
+                slot_of_[in_off_[r] + i] = slot;
+                orig_.push_back(i);
+                qs_.push_back((float)(s.q[i] * sqk));
+                lj_.push_back(make_float2((float)(0.5 * s.sig[i]), (float)(2.0 * std::sqrt(s.eps[i]))));
+                displ_sorted_.push_back(make_float4((float)s.displ[3 * i], (float)s.displ[3 * i + 1],
+                                                    (float)s.displ[3 * i + 2], 0.f));
+                slot++;
+            }
+            while (slot % kTile) {
+                orig_.push_back(-1);
+                qs_.push_back(0.f);
+                lj_.push_back(make_float2(0.f, 0.f));
+                displ_sorted_.push_back(displ_sorted_.back());
+                slot++;
+            }
+        }
+        rd.slot_end = slot;
+        rd.block_end = slot / kTile;
+        if (rd.mov_block_begin < 0) rd.mov_block_begin = rd.block_end;
+        for (int b = rd.block_begin; b < rd.block_end; b++) {
+            block_rep_.push_back(r);
+            int o = orig_[b * kTile];
+            int c = cls[o];
+            block_cls_.push_back(c);
+            block_d_.push_back(make_float4((float)cls_d[c][0], (float)cls_d[c][1], (float)cls_d[c][2], 0.f));
+        }
+        blk_ex.resize(rd.block_end);
+        blk_dx.resize(rd.block_end);
+
+        // exclusion tiles: masks (bit k of word l: pair (l, (l+k)&31) is computed)
+        std::map<std::pair<int, int>, int> tile_mask;
+        auto get_mask = [&](int bi, int bj) {
+            auto it = tile_mask.find({bi, bj});
+            if (it != tile_mask.end()) return it->second;
+            int id = (int)(masks_.size() / 32);
+            masks_.resize(masks_.size() + 32, 0xffffffffu);
+            tile_mask[{bi, bj}] = id;
+            return id;
+        };
+        for (int b = rd.block_begin; b < rd.block_end; b++) {
+            int id = get_mask(b, b);
+            for (int l = 0; l < 32; l++) {
+                uint32_t& w = masks_[(size_t)id * 32 + l];
+                w &= ~1u;  // self
+                bool pl = orig_[b * kTile + l] < 0;
+                for (int k = 0; k < 32; k++) {
+                    int lj2 = (l + k) & 31;
+                    if (pl || orig_[b * kTile + lj2] < 0) w &= ~(1u << k);
+                }
+            }
+        }
+        std::map<std::pair<int, int>, int> cross_mask;
+        std::unordered_set<uint64_t> seen;
+        for (const Exception& e : s.exc) {
+            int a = std::min(e.i, e.j), b2 = std::max(e.i, e.j);
+            uint64_t key = ((uint64_t)a << 32) | (uint64_t)b2;
+            if (!seen.insert(key).second) throw Error(1, "Multiple exceptions are specified for one particle pair");
+            int si = slot_local[e.i], sj = slot_local[e.j];
+            int bi = si / kTile, bj = sj / kTile, li = si % kTile, lj = sj % kTile;
+            if (bi > bj || (bi == bj && li > lj)) {
+                std::swap(bi, bj);
+                std::swap(li, lj);
+            }
+            int id = get_mask(bi, bj);
+            masks_[(size_t)id * 32 + li] &= ~(1u << ((lj - li) & 31));
+            if (bi == bj) masks_[(size_t)id * 32 + lj] &= ~(1u << ((li - lj) & 31));
+            // a pair whose atoms move differently is also masked in the difference tiles
+            int ci = cls[e.i], cj = cls[e.j];
+            if (ci != cj && !full_) {
+                int si2 = slot_local[e.i], sj2 = slot_local[e.j];
+                // the row belongs to the moving atom with the smaller class (non-moving = 0 never owns a row)
+                if (ci == 0 || (cj != 0 && cj < ci)) {
+                    std::swap(si2, sj2);
+                    std::swap(ci, cj);
+                }
+                int rbi = si2 / kTile, rbj = sj2 / kTile, rli = si2 % kTile, rlj = sj2 % kTile;
+                auto it = cross_mask.find({rbi, rbj});
+                int cid;
+                if (it == cross_mask.end()) {
+                    cid = (int)(masks_.size() / 32);
+                    masks_.resize(masks_.size() + 32, 0xffffffffu);
+                    cross_mask[{rbi, rbj}] = cid;
+                } else {
+                    cid = it->second;
+                }
+                masks_[(size_t)cid * 32 + rli] &= ~(1u << ((rlj - rli) & 31));
+            }
+        }
+        for (auto& kv : tile_mask) blk_ex[kv.first.first].push_back({kv.first.second, kv.second});
+        for (auto& kv : cross_mask) blk_dx[kv.first.first].push_back({kv.first.second, kv.second});
+
+        // exceptions, user-order indices
+        rd.exc_cta_b = (int)exc_cta_first_.size();
+        int first_exc = (int)exc_ij_.size();
+        for (const Exception& e : s.exc) {
+            bool cross = cls[e.i] != cls[e.j];
+            exc_ij_.push_back(make_int4(in_off_[r] + e.i, in_off_[r] + e.j, r, cross ? 1 : 0));
+            exc_p_.push_back(ExcParam{e.qq * kOne4PiEps0, e.sig, e.eps, kOne4PiEps0 * s.q[e.i] * s.q[e.j]});
+        }
+        for (int k = first_exc; k < (int)exc_ij_.size(); k += 256) exc_cta_first_.push_back(k);
+        rd.exc_cta_e = (int)exc_cta_first_.size();
+
+        // box and constants
+        for (int a = 0; a < 3; a++) {
+            rd.box[a] = (float)s.box[a];
+            rd.ibox[a] = (float)(1.0 / s.box[a]);
+            rd.boxd[a] = s.box[a];
+            rd.K[a] = s.grid[a];
+        }
+        double q2 = 0;
+        for (int i = 0; i < s.n; i++) q2 += s.q[i] * s.q[i];
+        rd.e_self = (method_ == NonbondedForce::PME) ? -kOne4PiEps0 * alpha_ / std::sqrt(kPi) * q2 : 0.0;
+        rd.var_nb = s.var_nb ? 1 : 0;
+    }
+    exc_cta_first_.push_back((int)exc_ij_.size());
+    NA_ = slot;
+    NB_ = slot / kTile;
+
+    // exclusion CSR
+    ex_start_.assign(NB_ + 1, 0);
+    dx_start_.assign(NB_ + 1, 0);
+    ex_ent_.clear();
+    dx_ent_.clear();
+    for (int b = 0; b < NB_; b++) {
+        std::sort(blk_ex[b].begin(), blk_ex[b].end());
+        std::sort(blk_dx[b].begin(), blk_dx[b].end());
+        ex_start_[b] = (int)ex_ent_.size();
+        for (auto& e : blk_ex[b]) ex_ent_.push_back(make_int2(e.first, e.second));
+        dx_start_[b] = (int)dx_ent_.size();
+        for (auto& e : blk_dx[b]) dx_ent_.push_back(make_int2(e.first, e.second));
+    }
+    ex_start_[NB_] = (int)ex_ent_.size();
+    dx_start_[NB_] = (int)dx_ent_.size();
+    if (masks_.empty()) masks_.resize(32, 0xffffffffu);
+
+    // rows: all state-1 rows, then state-2 rows (full) or the difference rows
+    row_desc_.clear();
+    for (int b = 0; b < NB_; b++) row_desc_.push_back(make_int4(b, ROW_STATE1, block_rep_[b], 0));
+    for (int r = 0; r < R_; r++) {
+        rep_host_[r].row1_b = rep_host_[r].block_begin;
+        rep_host_[r].row1_e = rep_host_[r].block_end;
+    }
+    for (int r = 0; r < R_; r++) {
+        RepDev& rd = rep_host_[r];
+        rd.row2_b = (int)row_desc_.size();
+        if (full_) {
+            for (int b = rd.block_begin; b < rd.block_end; b++) row_desc_.push_back(make_int4(b, ROW_STATE2, r, 0));
+        } else {
+            for (int b = rd.mov_block_begin; b < rd.block_end; b++) {
+                row_desc_.push_back(make_int4(b, ROW_DIFF1, r, 0));
+                row_desc_.push_back(make_int4(b, ROW_DIFF2, r, 0));
+            }
+        }
+        rd.row2_e = (int)row_desc_.size();
+    }
+    nrows_ = (int)row_desc_.size();
+
+    // PME grids grouped by dimensions (one batched cuFFT plan per group)
+    n_real_ = n_cplx_ = 0;
+    moduli_.clear();
+    conv_cta_rep_.clear();
+    conv_cta_first_.clear();
+    for (auto& g : groups_) {
+        if (g.fwd) cufftDestroy(g.fwd);
+        if (g.inv) cufftDestroy(g.inv);
+    }
+    groups_.clear();
+    if (method_ == NonbondedForce::PME) {
+        std::vector<int> order(R_);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            const int* a = specs_[x].grid;
+            const int* b = specs_[y].grid;
+            return std::lexicographical_compare(a, a + 3, b, b + 3);
+        });
+        for (int r : order) {
+            RepDev& rd = rep_host_[r];
+            if (groups_.empty() || std::memcmp(groups_.back().K, rd.K, sizeof(rd.K)) != 0) {
+                FftGroup g;
+                std::memcpy(g.K, rd.K, sizeof(g.K));
+                g.first_rep = r;
+                g.count = 0;
+                g.real_off = n_real_;
+                g.cplx_off = n_cplx_;
+                groups_.push_back(g);
+            }
+            groups_.back().count++;
+            long long G3 = (long long)rd.K[0] * rd.K[1] * rd.K[2];
+            long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
+            rd.real_off = n_real_;
+            rd.fixed_off = n_real_;
+            rd.cplx_off = n_cplx_;
+            n_real_ += 2 * G3;
+            n_cplx_ += 2 * C3;
+            for (int a = 0; a < 3; a++) {
+                std::vector<double> m;
+                bspline_moduli(rd.K[a], m);
+                rd.mod_off[a] = (int)moduli_.size();
+                for (double v : m) moduli_.push_back((float)v);
+            }
+        }
+        for (int r = 0; r < R_; r++) {
+            RepDev& rd = rep_host_[r];
+            long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
+            rd.conv_cta_b = (int)conv_cta_rep_.size();
+            const long long per = 4096;
+            for (long long k = 0; k < C3; k += per) {
+                conv_cta_rep_.push_back(r);
+                conv_cta_first_.push_back(k);
+            }
+            rd.conv_cta_e = (int)conv_cta_rep_.size();
+        }
+    } else {
+        for (int r = 0; r < R_; r++) {
+            rep_host_[r].conv_cta_b = rep_host_[r].conv_cta_e = 0;
+        }
+    }
+    for (int r = 0; r < R_; r++) {
+        const ReplicaSpec& s = specs_[r];
+        rep_host_[r].e_disp = 0.0;
+        if (s.dispersion) rep_host_[r].e_disp = dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]);
+    }
+    if (tile_cap_ == 0) tile_cap_ = nrows_ * 40 + 4096;
+    layout_ready_ = true;
+}
+
+// ---------------------------------------------------------------------------
+// Device buffers
+// ---------------------------------------------------------------------------
+
+void Engine::free_device() {
+    for (void* p : d_allocs_) cudaFree(p);
+    d_allocs_.clear();
+}
+
+template <typename T>
+static T* dalloc(std::vector<void*>& list, size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    CUDA_CHECK(cudaMalloc(&p, n * sizeof(T)));
+    list.push_back(p);
+    return (T*)p;
+}
+
+template <typename T>
+static T* dupload(std::vector<void*>& list, const std::vector<T>& v) {
+    T* p = dalloc<T>(list, v.size());
+    if (!v.empty()) CUDA_CHECK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+}
+
+void Engine::alloc_device() {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    destroy_graphs();
+    free_device();
+    Args& a = A_;
+    a = Args{};
+    a.R = R_;
+    a.NA = NA_;
+    a.NB = NB_;
+    a.nrows = nrows_;
+    a.row_cap = row_cap_;
+    a.tile_cap = tile_cap_;
+    a.n_in = n_in_;
+    a.full = full_ ? 1 : 0;
+    a.method = method_;
+    a.rc2 = (float)(cutoff_ * cutoff_);
+    a.alpha = (float)alpha_;
+    a.krf = (float)krf_;
+    a.crf = (float)crf_;
+    a.alphad = alpha_;
+    a.cutoffd = cutoff_;
+    a.reps = dalloc<RepDev>(d_allocs_, R_);
+    a.pos_in = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
+    {
+        std::vector<double> d(3 * (size_t)n_in_);
+        for (int r = 0; r < R_; r++)
+            std::memcpy(d.data() + 3 * (size_t)in_off_[r], specs_[r].displ.data(), sizeof(double) * 3 * specs_[r].n);
+        a.displ_in = dupload(d_allocs_, d);
+    }
+    a.slot_of = dupload(d_allocs_, slot_of_);
+    a.f_out = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
+    a.f_nb = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
+    a.orig = dupload(d_allocs_, orig_);
+    a.qs = dupload(d_allocs_, qs_);
+    a.lj = dupload(d_allocs_, lj_);
+    a.displ = dupload(d_allocs_, displ_sorted_);
+    a.posq = dalloc<float4>(d_allocs_, NA_);
+    a.posq2 = full_ ? dalloc<float4>(d_allocs_, NA_) : nullptr;
+    a.block_rep = dupload(d_allocs_, block_rep_);
+    a.block_cls = dupload(d_allocs_, block_cls_);
+    a.block_d = dupload(d_allocs_, block_d_);
+    a.bb_c = dalloc<float4>(d_allocs_, NB_);
+    a.bb_h = dalloc<float4>(d_allocs_, NB_);
+    a.bb_c2 = full_ ? dalloc<float4>(d_allocs_, NB_) : nullptr;
+    a.bb_h2 = full_ ? dalloc<float4>(d_allocs_, NB_) : nullptr;
+    a.row_desc = dupload(d_allocs_, row_desc_);
+    a.row_count = dalloc<int>(d_allocs_, nrows_);
+    a.ex_start = dupload(d_allocs_, ex_start_);
+    a.ex_ent = dupload(d_allocs_, ex_ent_);
+    a.dx_start = dupload(d_allocs_, dx_start_);
+    a.dx_ent = dupload(d_allocs_, dx_ent_);
+    a.masks = dupload(d_allocs_, masks_);
+    a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
+    a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
+    a.status = dalloc<Status>(d_allocs_, 1);
+    a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);
+    a.n_exc = (int)exc_ij_.size();
+    a.exc_ij = dupload(d_allocs_, exc_ij_);
+    a.exc_p = dupload(d_allocs_, exc_p_);
+    a.exc_ctas = (int)exc_cta_first_.size() - 1;
+    a.exc_cta_first = dupload(d_allocs_, exc_cta_first_);
+    a.e_part_exc = dalloc<double>(d_allocs_, 3 * (size_t)std::max(1, a.exc_ctas));
+    a.n_real_total = n_real_;
+    if (method_ == NonbondedForce::PME) {
+        a.qfix = dalloc<unsigned long long>(d_allocs_, n_real_);
+        CUDA_CHECK(cudaMemset(a.qfix, 0, sizeof(unsigned long long) * n_real_));
+        a.qreal = dalloc<float>(d_allocs_, n_real_);
+        a.qcplx = dalloc<float2>(d_allocs_, n_cplx_);
+        a.moduli = dupload(d_allocs_, moduli_);
+        a.conv_ctas = (int)conv_cta_rep_.size();
+        a.conv_cta_rep = dupload(d_allocs_, conv_cta_rep_);
+        // per-CTA [first, last) element ranges within each replica's spectrum
+        std::vector<long long> pairs(2 * conv_cta_rep_.size());
+        for (size_t c = 0; c < conv_cta_rep_.size(); c++) {
+            int r = conv_cta_rep_[c];
+            const RepDev& rd = rep_host_[r];
+            long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
+            bool last = (c + 1 == conv_cta_rep_.size()) || conv_cta_rep_[c + 1] != r;
+            pairs[2 * c] = conv_cta_first_[c];
+            pairs[2 * c + 1] = last ? C3 : conv_cta_first_[c + 1];
+        }
+        a.conv_cta_first = dupload(d_allocs_, pairs);
+        a.e_part_conv = dalloc<double>(d_allocs_, 2 * (size_t)std::max(1, a.conv_ctas));
+        for (auto& g : groups_) {
+            int n[3] = {g.K[0], g.K[1], g.K[2]};
+            long long G3 = (long long)n[0] * n[1] * n[2];
+            long long C3 = (long long)n[0] * n[1] * (n[2] / 2 + 1);
+            CUFFT_CHECK(cufftPlanMany(&g.fwd, 3, n, nullptr, 1, (int)G3, nullptr, 1, (int)C3, CUFFT_R2C, 2 * g.count));
+            CUFFT_CHECK(cufftPlanMany(&g.inv, 3, n, nullptr, 1, (int)C3, nullptr, 1, (int)G3, CUFFT_C2R, 2 * g.count));
+            CUFFT_CHECK(cufftSetStream(g.fwd, s_pme_));
+            CUFFT_CHECK(cufftSetStream(g.inv, s_pme_));
+        }
+    } else {
+        a.conv_ctas = 0;
+    }
+    a.results = dalloc<double>(d_allocs_, (size_t)R_ * NUM_RES);
+    a.matrix = dalloc<double>(d_allocs_, (size_t)R_ * R_);
+    a.beta = dalloc<double>(d_allocs_, 1);
+    CUDA_CHECK(cudaMemset(a.status, 0, sizeof(Status)));
+}
+
+void Engine::update_rep_table() {
+    for (int r = 0; r < R_; r++) {
+        RepDev& rd = rep_host_[r];
+        const ReplicaSpec& s = specs_[r];
+        for (int a = 0; a < 3; a++) {
+            rd.box[a] = (float)s.box[a];
+            rd.ibox[a] = (float)(1.0 / s.box[a]);
+            rd.boxd[a] = s.box[a];
+        }
+        for (int k = 0; k < NUM_GLOBALS; k++) rd.params[k] = s.params[k];
+        rd.e_disp = s.dispersion ? dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]) : 0.0;
+    }
+    std::memcpy(h_reps_, rep_host_.data(), sizeof(RepDev) * (size_t)R_);
+    *h_beta_ = beta_;
+}
+
+// ---------------------------------------------------------------------------
+// One evaluation: the kernel sequence (captured once into a CUDA graph)
+// ---------------------------------------------------------------------------
+
+int Engine::launches_per_eval() const {
+    // prepare, find, tiles, exceptions, finalize, output, matrix (+ PME kernels)
+    int n = 4 + 3;
+    if (method_ == NonbondedForce::PME) n += 4;
+    return n;
+}
+
+void Engine::record(cudaStream_t st, bool host_io) {
+    const Args& a = A_;
+    if (host_io) {
+        CUDA_CHECK(cudaMemcpyAsync((void*)a.pos_in, h_pos_, sizeof(double) * 3 * (size_t)n_in_,
+                                   cudaMemcpyHostToDevice, st));
+    }
+    CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_prepare(a, st);
+    bool pme = method_ == NonbondedForce::PME;
+    if (pme) {
+        CUDA_CHECK(cudaEventRecord(ev_fork_, st));
+        CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork_, 0));
+        launch_spread(a, s_pme_);
+        launch_convert(a, s_pme_);
+        for (auto& g : groups_)
+            CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
+        launch_conv(a, s_pme_);
+        for (auto& g : groups_)
+            CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
+        launch_gather(a, s_pme_);
+        CUDA_CHECK(cudaEventRecord(ev_join_, s_pme_));
+    }
+    launch_find(a, st);
+    launch_tiles(a, tile_grid_, st);
+    launch_exceptions(a, st);
+    if (pme) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
+    launch_finalize(a, st);
+    launch_output(a, st);
+    launch_matrix(a, st);
+    if (host_io) {
+        CUDA_CHECK(cudaMemcpyAsync(h_results_, a.results, sizeof(double) * NUM_RES * (size_t)R_,
+                                   cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(h_forces_, a.f_out, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost,
+                                   st));
+        CUDA_CHECK(cudaMemcpyAsync(h_fnb_, a.f_nb, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(h_matrix_, a.matrix, sizeof(double) * (size_t)R_ * R_, cudaMemcpyDeviceToHost,
+                                   st));
+    }
+    CUDA_CHECK(cudaMemcpyAsync(h_status_, a.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
+}
+
+bool Engine::check_status_and_grow() {
+    const Status& s = *h_status_;
+    if (!s.overflow) return false;
+    if (s.overflow & 2) {
+        int want = (int)(s.max_row * 1.25) + 8;
+        if (want > 1024) throw Error(6, "A tile row exceeds 1024 tiles: cutoff too large for the block layout");
+        row_cap_ = std::max(row_cap_, want);
+    }
+    if (s.overflow & 1) tile_cap_ = (int)(std::max(tile_cap_, s.tile_count) * 1.5) + 4096;
+    alloc_device();
+    return true;
+}
+
+void Engine::run(bool host_io, cudaStream_t user, const double* d_pos) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    if (!layout_ready_) {
+        build_layout();
+        alloc_device();
+    }
+    for (int attempt = 0; attempt < 4; attempt++) {
+        update_rep_table();
+        cudaStream_t st = user ? user : s_main_;
+        if (d_pos)
+            CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
+                                       cudaMemcpyDeviceToDevice, st));
+        if (profiling_) {
+            // eager launches bracketed by events, one stream, for per-kernel timings
+            times_.clear();
+            std::vector<cudaEvent_t> ev;
+            auto mark = [&](const char* name) {
+                cudaEvent_t e;
+                CUDA_CHECK(cudaEventCreate(&e));
+                CUDA_CHECK(cudaEventRecord(e, st));
+                ev.push_back(e);
+                times_.push_back({name, 0.0});
+            };
+            const Args& a = A_;
+            if (host_io)
+                CUDA_CHECK(cudaMemcpyAsync((void*)a.pos_in, h_pos_, sizeof(double) * 3 * (size_t)n_in_,
+                                           cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
+            mark("start");
+            launch_prepare(a, st);
+            mark("prepare");
+            launch_find(a, st);
+            mark("find");
+            launch_tiles(a, tile_grid_, st);
+            mark("tiles");
+            launch_exceptions(a, st);
+            mark("exceptions");
+            if (method_ == NonbondedForce::PME) {
+                for (auto& g : groups_) {
+                    CUFFT_CHECK(cufftSetStream(g.fwd, st));
+                    CUFFT_CHECK(cufftSetStream(g.inv, st));
+                }
+                launch_spread(a, st);
+                mark("spread");
+                launch_convert(a, st);
+                mark("convert");
+                for (auto& g : groups_)
+                    CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
+                mark("fft_r2c");
+                launch_conv(a, st);
+                mark("conv");
+                for (auto& g : groups_)
+                    CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
+                mark("fft_c2r");
+                launch_gather(a, st);
+                mark("gather");
+                for (auto& g : groups_) {
+                    CUFFT_CHECK(cufftSetStream(g.fwd, s_pme_));
+                    CUFFT_CHECK(cufftSetStream(g.inv, s_pme_));
+                }
+            }
+            launch_finalize(a, st);
+            mark("finalize");
+            launch_output(a, st);
+            mark("output");
+            launch_matrix(a, st);
+            mark("matrix");
+            if (host_io) {
+                CUDA_CHECK(cudaMemcpyAsync(h_results_, a.results, sizeof(double) * NUM_RES * (size_t)R_,
+                                           cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaMemcpyAsync(h_forces_, a.f_out, sizeof(double) * 3 * (size_t)n_in_,
+                                           cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaMemcpyAsync(h_fnb_, a.f_nb, sizeof(double) * 3 * (size_t)n_in_,
+                                           cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaMemcpyAsync(h_matrix_, a.matrix, sizeof(double) * (size_t)R_ * R_,
+                                           cudaMemcpyDeviceToHost, st));
+            }
+            CUDA_CHECK(cudaMemcpyAsync(h_status_, a.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            for (size_t k = 1; k < ev.size(); k++) {
+                float ms = 0;
+                CUDA_CHECK(cudaEventElapsedTime(&ms, ev[k - 1], ev[k]));
+                times_[k].ms = ms;
+            }
+            for (auto e : ev) cudaEventDestroy(e);
+            times_.erase(times_.begin());
+        } else {
+            cudaGraphExec_t& gx = host_io ? graph_host_ : graph_dev_;
+            if (!gx) {
+                cudaGraph_t g;
+                CUDA_CHECK(cudaStreamBeginCapture(s_main_, cudaStreamCaptureModeThreadLocal));
+                try {
+                    record(s_main_, host_io);
+                } catch (...) {
+                    cudaStreamEndCapture(s_main_, &g);
+                    throw;
+                }
+                CUDA_CHECK(cudaStreamEndCapture(s_main_, &g));
+                CUDA_CHECK(cudaGraphInstantiate(&gx, g, 0));
+                CUDA_CHECK(cudaGraphDestroy(g));
+            }
+            CUDA_CHECK(cudaGraphLaunch(gx, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+        }
+        if (!check_status_and_grow()) return;
+    }
+    throw Error(6, "Tile list capacity could not be established");
+}
+
+void Engine::evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix) {
+    run(true, nullptr, nullptr);
+    for (int r = 0; r < R_; r++) {
+        if (energies) energies[r] = h_results_[(size_t)r * NUM_RES + RES_ENERGY];
+    }
+    if (forces) std::memcpy(forces, h_forces_, sizeof(double) * 3 * (size_t)n_in_);
+    if (forces_nb) std::memcpy(forces_nb, h_fnb_, sizeof(double) * 3 * (size_t)n_in_);
+    if (results) std::memcpy(results, h_results_, sizeof(double) * NUM_RES * (size_t)R_);
+    if (matrix) std::memcpy(matrix, h_matrix_, sizeof(double) * (size_t)R_ * R_);
+}
+
+void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    if (!layout_ready_) {
+        // the layout is built from positions: take them to the host once
+        CUDA_CHECK(cudaMemcpyAsync(h_pos_, d_pos, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        build_layout();
+        alloc_device();
+    }
+    run(false, stream, d_pos);
+    if (d_forces)
+        CUDA_CHECK(cudaMemcpyAsync(d_forces, A_.f_out, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToDevice,
+                                   stream));
+    if (d_results)
+        CUDA_CHECK(cudaMemcpyAsync(d_results, A_.results, sizeof(double) * NUM_RES * (size_t)R_,
+                                   cudaMemcpyDeviceToDevice, stream));
+    CUDA_CHECK(cudaMemcpyAsync(h_results_, A_.results, sizeof(double) * NUM_RES * (size_t)R_, cudaMemcpyDeviceToHost,
+                               stream));
+    CUDA_CHECK(cudaStreamSynchronize(stream));
+}
+
+void Engine::reorder() { layout_ready_ = false; }
+
+}  // namespace atm

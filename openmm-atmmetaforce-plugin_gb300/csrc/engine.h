@@ -1,0 +1,146 @@
+// GPU evaluation engine for R replicas of the ATM path (one CUDA graph per
+// evaluation).  A single context is an engine with R = 1.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "model.h"
+
+namespace atm {
+
+// Everything one replica contributes, copied out of its System.
+struct ReplicaSpec {
+    int n = 0;
+    std::vector<double> q, sig, eps;
+    std::vector<Exception> exc;
+    std::vector<double> displ;  // 3n
+    int method = 0;
+    double cutoff = 1.0, epsRF = 78.3, alpha = 0.0;
+    int grid[3] = {0, 0, 0};
+    bool dispersion = false;
+    double box[3] = {0, 0, 0};
+    double params[NUM_GLOBALS] = {0};
+    bool var_nb = true;
+};
+
+// Build a ReplicaSpec from a System holding one NonbondedForce and one
+// ATMMetaForce (the inner-system copy of ATMMetaForceImpl.cpp:77-112).
+ReplicaSpec spec_from_system(const System& sys);
+
+struct KernelTime {
+    std::string name;
+    double ms;
+};
+
+class Engine {
+public:
+    Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    int replicas() const { return R_; }
+    int atoms(int r) const { return specs_[r].n; }
+    int in_offset(int r) const { return in_off_[r]; }
+    int total_atoms() const { return n_in_; }
+    bool full_mode() const { return full_; }
+
+    void set_positions(int r, const double* pos);
+    void set_all_positions(const double* pos);
+    void set_box(int r, const double* box);
+    void set_param(int r, int which, double v);
+    double param(int r, int which) const { return specs_[r].params[which]; }
+    void set_displacements(int r, const double* displ);  // 3n, particle count unchanged
+    void set_beta(double beta) { beta_ = beta; }
+
+    // Host path: positions from the staging copy; outputs to host (nullable).
+    void evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix);
+    // Device path on the caller's stream.
+    void evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream);
+
+    // Re-sort atoms from the current positions (exclusion masks follow).
+    void reorder();
+
+    void set_profiling(bool on) { profiling_ = on; }
+    const std::vector<KernelTime>& kernel_times() const { return times_; }
+    int launches_per_eval() const;
+
+private:
+    void build_layout();
+    void alloc_device();
+    void free_device();
+    void upload_static();
+    void fill_args();
+    void update_rep_table();
+    void record(cudaStream_t main, bool host_io);
+    void run(bool host_io, cudaStream_t user, const double* d_pos);
+    bool check_status_and_grow();
+    void destroy_graphs();
+
+    int R_ = 0, dev_ = 0;
+    bool full_ = false;
+    std::vector<ReplicaSpec> specs_;
+    std::vector<int> in_off_;
+    int n_in_ = 0;
+    int NA_ = 0, NB_ = 0, nrows_ = 0;
+    int row_cap_ = 96;
+    int tile_cap_ = 0;
+    int method_ = 0;
+    double cutoff_ = 1.0, alpha_ = 0.0, krf_ = 0.0, crf_ = 0.0;
+    double beta_ = 1.0;
+    bool layout_ready_ = false;
+    bool profiling_ = false;
+    int tile_grid_ = 0;
+
+    // host copies of the layout
+    std::vector<int> orig_, slot_of_, block_rep_, block_cls_;
+    std::vector<float> qs_;
+    std::vector<float2> lj_;
+    std::vector<float4> displ_sorted_, block_d_;
+    std::vector<int4> row_desc_;
+    std::vector<int> ex_start_, dx_start_;
+    std::vector<int2> ex_ent_, dx_ent_;
+    std::vector<uint32_t> masks_;
+    std::vector<int4> exc_ij_;
+    std::vector<ExcParam> exc_p_;
+    std::vector<int> exc_cta_first_;
+    std::vector<int> conv_cta_rep_;
+    std::vector<long long> conv_cta_first_;
+    std::vector<float> moduli_;
+    std::vector<RepDev> rep_host_;
+    long long n_real_ = 0, n_cplx_ = 0;
+    struct FftGroup {
+        int K[3];
+        int first_rep, count;
+        cufftHandle fwd = 0, inv = 0;
+        long long real_off, cplx_off;
+    };
+    std::vector<FftGroup> groups_;
+
+    // pinned host staging
+    double* h_pos_ = nullptr;      // 3*n_in
+    double* h_forces_ = nullptr;   // 3*n_in
+    double* h_fnb_ = nullptr;      // 3*n_in
+    double* h_results_ = nullptr;  // R*NUM_RES
+    double* h_matrix_ = nullptr;   // R*R
+    RepDev* h_reps_ = nullptr;     // R
+    double* h_beta_ = nullptr;
+    Status* h_status_ = nullptr;
+
+    // device buffers
+    Args A_{};
+    void* d_mem_ = nullptr;
+    std::vector<void*> d_allocs_;
+
+    cudaStream_t s_main_ = nullptr, s_pme_ = nullptr;
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+    cudaGraphExec_t graph_host_ = nullptr, graph_dev_ = nullptr;
+    std::vector<KernelTime> times_;
+};
+
+}  // namespace atm

@@ -1,0 +1,883 @@
+// CUDA kernels of the ATM evaluation path (sm_103a).
+//
+// Data flow of one evaluation of R replicas:
+//   prepare  : user positions (FP64) -> wrapped float4 slots, state-2 copies,
+//              block bounding boxes; zero the force accumulators
+//   find     : one warp per tile row -> compacted list of interacting 32x32 tiles
+//   tiles    : persistent warps over the tile list: LJ + reaction field / Ewald
+//              direct space, tile rotation by warp shuffles, fixed-point forces
+//   exceptions: exception pairs and Ewald exclusion corrections in FP64
+//   spread / convert / (cuFFT R2C) / conv / (cuFFT C2R) / gather : smooth PME
+//   finalize : FP64 energies, soft-core + softplus merge (ATM scalars)
+//   output   : hybrid forces F1 + s' (F2 - F1) in user order
+//   matrix   : replicas x states reduced-energy matrix
+//
+// Reference semantics: inner evaluations of ATMMetaForceImpl.cpp:113,116; the
+// displacement of CopyState, platforms/common/src/kernels/atmmetaforce.cc:19-52;
+// the merge of ReferenceATMMetaForceKernels.cpp:56-113 (FP64, as the Reference
+// platform, instead of the float `sp` of CommonATMMetaForceKernels.cpp:199).
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.cuh"
+
+namespace atm {
+
+#define FULL_MASK 0xffffffffu
+
+__device__ __forceinline__ void fix_add(unsigned long long* p, float v) {
+    // cvt.rni.s64.f32 saturates out-of-range values; the sum of two's-complement
+    // integers is exact and order independent
+    atomicAdd(p, (unsigned long long)__float2ll_rn(v * kFixScaleF));
+}
+
+__device__ __forceinline__ void fix_add_d(unsigned long long* p, double v) {
+    atomicAdd(p, (unsigned long long)__double2ll_rn(v * kFixScale));
+}
+
+__device__ __forceinline__ float wrapf(float x, float L, float iL) { return x - L * floorf(x * iL); }
+
+// ---------------------------------------------------------------------------
+// prepare: one warp per block
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void warp_bbox(float x, float y, float z, const RepDev& R, float4* c, float4* h,
+                                          int lane) {
+    float x0 = __shfl_sync(FULL_MASK, x, 0), y0 = __shfl_sync(FULL_MASK, y, 0), z0 = __shfl_sync(FULL_MASK, z, 0);
+    float dx = x - x0, dy = y - y0, dz = z - z0;
+    dx -= R.box[0] * rintf(dx * R.ibox[0]);
+    dy -= R.box[1] * rintf(dy * R.ibox[1]);
+    dz -= R.box[2] * rintf(dz * R.ibox[2]);
+    float lx = dx, ly = dy, lz = dz, hx = dx, hy = dy, hz = dz;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(FULL_MASK, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(FULL_MASK, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(FULL_MASK, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(FULL_MASK, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(FULL_MASK, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(FULL_MASK, hz, o));
+    }
+    if (lane == 0) {
+        *c = make_float4(x0 + 0.5f * (lx + hx), y0 + 0.5f * (ly + hy), z0 + 0.5f * (lz + hz), 0.f);
+        *h = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), 0.f);
+    }
+}
+
+__global__ void k_prepare(Args a) {
+    int lane = threadIdx.x & 31;
+    int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= a.NB) return;
+    int s = b * kTile + lane;
+    int rep = a.block_rep[b];
+    const RepDev& R = a.reps[rep];
+    int o = a.orig[s];
+    if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
+    const double* p = a.pos_in + 3 * (size_t)(R.in_off + o);
+    float x = (float)(p[0] - R.boxd[0] * floor(p[0] / R.boxd[0]));
+    float y = (float)(p[1] - R.boxd[1] * floor(p[1] / R.boxd[1]));
+    float z = (float)(p[2] - R.boxd[2] * floor(p[2] / R.boxd[2]));
+    float q = a.qs[s];
+    a.posq[s] = make_float4(x, y, z, q);
+    for (int k = 0; k < 6; k++) a.F[(size_t)k * a.NA + s] = 0ull;
+    warp_bbox(x, y, z, R, &a.bb_c[b], &a.bb_h[b], lane);
+    if (a.full) {
+        float4 d = a.displ[s];
+        float x2 = wrapf(x + d.x, R.box[0], R.ibox[0]);
+        float y2 = wrapf(y + d.y, R.box[1], R.ibox[1]);
+        float z2 = wrapf(z + d.z, R.box[2], R.ibox[2]);
+        a.posq2[s] = make_float4(x2, y2, z2, q);
+        warp_bbox(x2, y2, z2, R, &a.bb_c2[b], &a.bb_h2[b], lane);
+    }
+    if (b == 0 && lane == 0) {
+        a.status->tile_count = 0;
+        a.status->overflow = 0;
+        a.status->max_row = 0;
+    }
+}
+
+void launch_prepare(const Args& a, cudaStream_t s) {
+    int threads = 256;
+    int blocks = (a.NB * 32 + threads - 1) / threads;
+    k_prepare<<<blocks, threads, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// find: one warp per row; bounding-box test of block I against candidates J
+// ---------------------------------------------------------------------------
+constexpr int kFindWarps = 4;
+constexpr int kMaxRowCap = 1024;
+
+__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj, const RepDev& R, float rc2) {
+    float dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
+    dx -= R.box[0] * rintf(dx * R.ibox[0]);
+    dy -= R.box[1] * rintf(dy * R.ibox[1]);
+    dz -= R.box[2] * rintf(dz * R.ibox[2]);
+    dx = fmaxf(0.f, fabsf(dx) - hi.x - hj.x);
+    dy = fmaxf(0.f, fabsf(dy) - hi.y - hj.y);
+    dz = fmaxf(0.f, fabsf(dz) - hi.z - hj.z);
+    return dx * dx + dy * dy + dz * dz < rc2;
+}
+
+__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
+    __shared__ int2 stage[kFindWarps][kMaxRowCap];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int row = blockIdx.x * kFindWarps + w;
+    if (row >= a.nrows) return;
+    int4 d = a.row_desc[row];
+    int I = d.x, kind = d.y, rep = d.z;
+    const RepDev& R = a.reps[rep];
+    int2* st = stage[w];
+    int cap = a.row_cap < kMaxRowCap ? a.row_cap : kMaxRowCap;
+    bool diff = kind >= ROW_DIFF1;
+    bool g2 = kind == ROW_DIFF2;
+    const int* es = diff ? a.dx_start : a.ex_start;
+    const int2* ee = diff ? a.dx_ent : a.ex_ent;
+    int e0 = es[I], e1 = es[I + 1];
+    int n = 0;
+    // exclusion tiles first (always processed)
+    for (int k = e0 + lane; k < e1; k += 32) {
+        int pos = k - e0;
+        if (pos < cap) st[pos] = ee[k];
+    }
+    n = e1 - e0;
+    float4 ci, hi;
+    if (kind == ROW_STATE2) {
+        ci = a.bb_c2[I];
+        hi = a.bb_h2[I];
+    } else {
+        ci = a.bb_c[I];
+        hi = a.bb_h[I];
+        if (g2) {
+            float4 dd = a.block_d[I];
+            ci.x += dd.x;
+            ci.y += dd.y;
+            ci.z += dd.z;
+        }
+    }
+    int cls_i = a.block_cls[I];
+    int jb = diff ? R.block_begin : I + 1;
+    int je = R.block_end;
+    for (int base = jb; base < je; base += 32) {
+        int J = base + lane;
+        bool ok = false;
+        if (J < je) {
+            if (diff) {
+                int cj = a.block_cls[J];
+                ok = (J != I) && cj != cls_i && (cj == 0 || cls_i < cj);
+            } else {
+                ok = true;
+            }
+            if (ok) {
+                float4 cj4, hj4;
+                if (kind == ROW_STATE2) {
+                    cj4 = a.bb_c2[J];
+                    hj4 = a.bb_h2[J];
+                } else {
+                    cj4 = a.bb_c[J];
+                    hj4 = a.bb_h[J];
+                    if (g2 && a.block_cls[J] != 0) {
+                        float4 dd = a.block_d[J];
+                        cj4.x += dd.x;
+                        cj4.y += dd.y;
+                        cj4.z += dd.z;
+                    }
+                }
+                ok = boxes_close(ci, hi, cj4, hj4, R, a.rc2);
+            }
+            if (ok) {
+                for (int k = e0; k < e1; k++)
+                    if (ee[k].x == J) ok = false;
+            }
+        }
+        unsigned bal = __ballot_sync(FULL_MASK, ok);
+        if (ok) {
+            int pos = n + __popc(bal & ((1u << lane) - 1u));
+            if (pos < cap) st[pos] = make_int2(J, -1);
+        }
+        n += __popc(bal);
+    }
+    __syncwarp();
+    if (n > cap) {
+        if (lane == 0) {
+            atomicOr(&a.status->overflow, 2);
+            atomicMax(&a.status->max_row, n);
+        }
+        n = cap;
+    }
+    int tbase = 0;
+    if (lane == 0) tbase = atomicAdd(&a.status->tile_count, n);
+    tbase = __shfl_sync(FULL_MASK, tbase, 0);
+    if (lane == 0) a.row_count[row] = n;
+    if (tbase + n > a.tile_cap) {
+        if (lane == 0) atomicOr(&a.status->overflow, 1);
+        return;
+    }
+    for (int k = lane; k < n; k += 32) {
+        int2 e = st[k];
+        a.tiles[tbase + k] = make_int4(I, e.x, row | (kind << 28), (e.y + 1) | (k << 20));
+    }
+}
+
+void launch_find(const Args& a, cudaStream_t s) {
+    int blocks = (a.nrows + kFindWarps - 1) / kFindWarps;
+    k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// tiles: persistent warps, static stride over the tile list
+// ---------------------------------------------------------------------------
+
+// erfc(x) for x >= 0: Abramowitz & Stegun, Handbook of Mathematical Functions,
+// eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term.
+__device__ __forceinline__ float erfc_as(float x, float expmx2) {
+    float t = 1.0f / (1.0f + 0.3275911f * x);
+    float p = t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
+    return p * expmx2;
+}
+
+template <int METHOD>
+__device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float eps4, float alpha, float krf, float crf,
+                                          float& e, float& fr) {
+    float invr = rsqrtf(r2);
+    float invr2 = invr * invr;
+    float s2 = sig * sig * invr2;
+    float s6 = s2 * s2 * s2;
+    e = eps4 * (s6 * s6 - s6);
+    fr = eps4 * (12.0f * s6 * s6 - 6.0f * s6) * invr2;
+    if (METHOD == 4) {
+        float r = r2 * invr;
+        float ar = alpha * r;
+        float ex = __expf(-ar * ar);
+        float ec = erfc_as(ar, ex);
+        e += qq * ec * invr;
+        fr += qq * (ec * invr + 1.1283791670955126f * alpha * ex) * invr2;
+    } else {
+        e += qq * (invr + krf * r2 - crf);
+        fr += qq * (invr * invr2 - 2.0f * krf);
+    }
+}
+
+template <int METHOD>
+__global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int ntiles = a.status->tile_count;
+    if (ntiles > a.tile_cap) ntiles = a.tile_cap;
+    const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
+    for (int t = gw; t < ntiles; t += nw) {
+        const int4 T = a.tiles[t];
+        const int I = T.x, J = T.y;
+        const int row = T.z & 0x0fffffff, kind = (unsigned)T.z >> 28;
+        const int maskid = (T.w & 0xfffff) - 1, slot = (unsigned)T.w >> 20;
+        const int rep = a.block_rep[I];
+        const float Lx = a.reps[rep].box[0], Ly = a.reps[rep].box[1], Lz = a.reps[rep].box[2];
+        const float iLx = a.reps[rep].ibox[0], iLy = a.reps[rep].ibox[1], iLz = a.reps[rep].ibox[2];
+        const bool diff = kind >= ROW_DIFF1;
+        const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
+        const int i = I * kTile + lane;
+        const int j0 = J * kTile + lane;
+        float4 pi = P[i];
+        float4 pj = P[j0];
+        const float2 li = a.lj[i];
+        float2 lj = a.lj[j0];
+        if (kind == ROW_DIFF2) {
+            float4 di = a.displ[i], dj = a.displ[j0];
+            pi.x += di.x; pi.y += di.y; pi.z += di.z;
+            pj.x += dj.x; pj.y += dj.y; pj.z += dj.z;
+        }
+        const unsigned mask = maskid >= 0 ? a.masks[(size_t)maskid * 32 + lane] : FULL_MASK;
+        const bool diag = (I == J);
+        float fix = 0.f, fiy = 0.f, fiz = 0.f, fjx = 0.f, fjy = 0.f, fjz = 0.f;
+        float e32 = 0.f;
+        double e64 = 0.0;
+        const int src = (lane + 1) & 31;
+#pragma unroll 4
+        for (int k = 0; k < 32; k++) {
+            float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+            dx -= Lx * rintf(dx * iLx);
+            dy -= Ly * rintf(dy * iLy);
+            dz -= Lz * rintf(dz * iLz);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            if (((mask >> k) & 1u) && r2 < rc2) {
+                float e, fr;
+                pair_eval<METHOD>(r2, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
+                if (diff) e64 += (double)e;
+                else e32 += e;
+                float fx = fr * dx, fy = fr * dy, fz = fr * dz;
+                fix -= fx; fiy -= fy; fiz -= fz;
+                fjx += fx; fjy += fy; fjz += fz;
+            }
+            pj.x = __shfl_sync(FULL_MASK, pj.x, src);
+            pj.y = __shfl_sync(FULL_MASK, pj.y, src);
+            pj.z = __shfl_sync(FULL_MASK, pj.z, src);
+            pj.w = __shfl_sync(FULL_MASK, pj.w, src);
+            lj.x = __shfl_sync(FULL_MASK, lj.x, src);
+            lj.y = __shfl_sync(FULL_MASK, lj.y, src);
+            fjx = __shfl_sync(FULL_MASK, fjx, src);
+            fjy = __shfl_sync(FULL_MASK, fjy, src);
+            fjz = __shfl_sync(FULL_MASK, fjz, src);
+        }
+        double esum = diff ? e64 : (double)e32 * (diag ? 0.5 : 1.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+        float sign = 1.0f;
+        if (kind == ROW_DIFF1) {
+            sign = -1.0f;
+            esum = -esum;
+        }
+        if (lane == 0) a.e_tile[(size_t)row * a.row_cap + slot] = esum;
+        unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
+        fix_add(Fp + i, sign * fix);
+        fix_add(Fp + a.NA + i, sign * fiy);
+        fix_add(Fp + 2 * (size_t)a.NA + i, sign * fiz);
+        if (!diag) {
+            int j = J * kTile + lane;
+            fix_add(Fp + j, sign * fjx);
+            fix_add(Fp + a.NA + j, sign * fjy);
+            fix_add(Fp + 2 * (size_t)a.NA + j, sign * fjz);
+        }
+    }
+}
+
+int tiles_kernel_blocks_per_sm() {
+    int n4 = 0, n2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2>, kTileThreads, 0);
+    return n4 < n2 ? n4 : n2;
+}
+
+void launch_tiles(const Args& a, int grid, cudaStream_t s) {
+    if (a.method == 4)
+        k_tiles<4><<<grid, kTileThreads, 0, s>>>(a);
+    else
+        k_tiles<2><<<grid, kTileThreads, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// exceptions: FP64, user-order positions; one CTA per 256 exceptions of a replica
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const ExcParam& p, double dx, double dy,
+                                           double dz, double* f) {
+    double r2 = dx * dx + dy * dy + dz * dz;
+    double e = 0.0, fr = 0.0;
+    if (p.x != 0.0 || p.z != 0.0) {
+        // nonzero exception: Coulomb chargeProd/r + LJ, no cutoff, no periodic image
+        double inv_r2 = 1.0 / r2, inv_r = sqrt(inv_r2);
+        e += p.x * inv_r;
+        fr += p.x * inv_r * inv_r2;
+        if (p.z != 0.0) {
+            double s2 = p.y * p.y * inv_r2;
+            double s6 = s2 * s2 * s2;
+            e += 4.0 * p.z * (s6 * s6 - s6);
+            fr += 4.0 * p.z * (12.0 * s6 * s6 - 6.0 * s6) * inv_r2;
+        }
+    }
+    f[0] = fr * dx;
+    f[1] = fr * dy;
+    f[2] = fr * dz;
+    if (a.method == 4) {
+        // Ewald exclusion correction at the minimum-image separation
+        double mx = dx - R.boxd[0] * rint(dx / R.boxd[0]);
+        double my = dy - R.boxd[1] * rint(dy / R.boxd[1]);
+        double mz = dz - R.boxd[2] * rint(dz / R.boxd[2]);
+        double m2 = mx * mx + my * my + mz * mz;
+        if (m2 > 0.0) {
+            double r = sqrt(m2);
+            double ar = a.alphad * r;
+            double ef = erf(ar);
+            e -= p.w * ef / r;
+            double fm = p.w * (1.1283791670955126 * a.alphad * exp(-ar * ar) - ef / r) / m2;
+            f[0] += fm * mx;
+            f[1] += fm * my;
+            f[2] += fm * mz;
+        } else {
+            e -= p.w * 1.1283791670955126 * a.alphad;
+        }
+    }
+    return e;
+}
+
+__global__ void __launch_bounds__(256) k_exceptions(Args a) {
+    __shared__ double red[3][256];
+    int c = blockIdx.x;
+    int e = a.exc_cta_first[c] + threadIdx.x;
+    double E1 = 0.0, E2 = 0.0, DE = 0.0;
+    if (e < a.exc_cta_first[c + 1]) {
+        int4 ij = a.exc_ij[e];
+        ExcParam p = a.exc_p[e];
+        const RepDev& R = a.reps[ij.z];
+        const double* xi = a.pos_in + 3 * (size_t)ij.x;
+        const double* xj = a.pos_in + 3 * (size_t)ij.y;
+        const double* di = a.displ_in + 3 * (size_t)ij.x;
+        const double* dj = a.displ_in + 3 * (size_t)ij.y;
+        int si = a.slot_of[ij.x], sj = a.slot_of[ij.y];
+        double f1[3], f2[3];
+        E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1);
+        for (int k = 0; k < 3; k++) {
+            fix_add_d(a.F + (size_t)k * a.NA + si, -f1[k]);
+            fix_add_d(a.F + (size_t)k * a.NA + sj, f1[k]);
+        }
+        if (a.full || ij.w) {
+            E2 = exc_term(a, R, p, (xj[0] + dj[0]) - (xi[0] + di[0]), (xj[1] + dj[1]) - (xi[1] + di[1]),
+                          (xj[2] + dj[2]) - (xi[2] + di[2]), f2);
+            if (!a.full) {
+                DE = E2 - E1;
+                E2 = 0.0;
+                for (int k = 0; k < 3; k++) f2[k] -= f1[k];
+            }
+            for (int k = 0; k < 3; k++) {
+                fix_add_d(a.F + (size_t)(3 + k) * a.NA + si, -f2[k]);
+                fix_add_d(a.F + (size_t)(3 + k) * a.NA + sj, f2[k]);
+            }
+        }
+    }
+    red[0][threadIdx.x] = E1;
+    red[1][threadIdx.x] = E2;
+    red[2][threadIdx.x] = DE;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int k = 0; k < 3; k++) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) a.e_part_exc[3 * c + threadIdx.x] = red[threadIdx.x][0];
+}
+
+void launch_exceptions(const Args& a, cudaStream_t s) {
+    if (a.exc_ctas > 0) k_exceptions<<<a.exc_ctas, 256, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// PME
+// ---------------------------------------------------------------------------
+
+// Order-5 cardinal B-spline weights w[k] = M5(t+k) and derivatives, by the
+// recursion M_m(x) = (x M_{m-1}(x) + (m-x) M_{m-1}(x-1)) / (m-1).
+__device__ __forceinline__ void bspline5(float t, float* w, float* dw) {
+    float a0 = t, a1 = 1.0f - t;
+    float b0 = 0.5f * t * a0, b1 = 0.5f * ((t + 1.0f) * a1 + (2.0f - t) * a0), b2 = 0.5f * (1.0f - t) * a1;
+    const float third = 1.0f / 3.0f;
+    float c0 = third * t * b0;
+    float c1 = third * ((t + 1.0f) * b1 + (3.0f - t) * b0);
+    float c2 = third * ((t + 2.0f) * b2 + (2.0f - t) * b1);
+    float c3 = third * (1.0f - t) * b2;
+    if (dw) {
+        dw[0] = c0;
+        dw[1] = c1 - c0;
+        dw[2] = c2 - c1;
+        dw[3] = c3 - c2;
+        dw[4] = -c3;
+    }
+    w[0] = 0.25f * t * c0;
+    w[1] = 0.25f * ((t + 1.0f) * c1 + (4.0f - t) * c0);
+    w[2] = 0.25f * ((t + 2.0f) * c2 + (3.0f - t) * c1);
+    w[3] = 0.25f * ((t + 3.0f) * c3 + (2.0f - t) * c2);
+    w[4] = 0.25f * (1.0f - t) * c3;
+}
+
+struct Stencil {
+    int base[3];
+    float w[3][5];
+    float dw[3][5];
+};
+
+__device__ __forceinline__ void make_stencil(float x, float y, float z, const RepDev& R, Stencil& S, bool deriv) {
+    float c[3] = {x, y, z};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        float f = c[d] * R.ibox[d];
+        f -= floorf(f);
+        float u = f * (float)R.K[d];
+        int b = (int)floorf(u);
+        float t = u - (float)b;
+        if (b >= R.K[d]) b -= R.K[d];
+        if (b < 0) b += R.K[d];
+        S.base[d] = b;
+        bspline5(t, S.w[d], deriv ? S.dw[d] : nullptr);
+    }
+}
+
+__device__ __forceinline__ void spread_one(unsigned long long* G, const RepDev& R, const Stencil& S, float q) {
+    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
+    int iz[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        int v = S.base[2] - c;
+        iz[c] = v < 0 ? v + Kz : v;
+    }
+#pragma unroll
+    for (int a0 = 0; a0 < 5; a0++) {
+        int ix = S.base[0] - a0;
+        if (ix < 0) ix += Kx;
+        float wa = q * S.w[0][a0];
+#pragma unroll
+        for (int b0 = 0; b0 < 5; b0++) {
+            int iy = S.base[1] - b0;
+            if (iy < 0) iy += Ky;
+            float wab = wa * S.w[1][b0];
+            size_t rowb = ((size_t)ix * Ky + iy) * Kz;
+#pragma unroll
+            for (int c0 = 0; c0 < 5; c0++) fix_add(G + rowb + iz[c0], wab * S.w[2][c0]);
+        }
+    }
+}
+
+__global__ void k_spread(Args a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.NA) return;
+    int b = s >> 5;
+    const RepDev& R = a.reps[a.block_rep[b]];
+    float4 p = a.posq[s];
+    if (p.w == 0.0f) return;
+    size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    unsigned long long* G1 = a.qfix + R.fixed_off;
+    unsigned long long* G2 = G1 + G3;
+    Stencil S;
+    make_stencil(p.x, p.y, p.z, R, S, false);
+    spread_one(G1, R, S, p.w);
+    if (a.full) {
+        float4 p2 = a.posq2[s];
+        make_stencil(p2.x, p2.y, p2.z, R, S, false);
+        spread_one(G2, R, S, p.w);
+    } else if (a.block_cls[b] != 0) {
+        // structure-factor update of the moving atoms: -q at x, +q at x + d
+        spread_one(G2, R, S, -p.w);
+        float4 d = a.displ[s];
+        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
+                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, false);
+        spread_one(G2, R, S, p.w);
+    }
+}
+
+void launch_spread(const Args& a, cudaStream_t s) {
+    k_spread<<<(a.NA + 127) / 128, 128, 0, s>>>(a);
+}
+
+// fixed-point charge grids -> float grids; clears the fixed-point grids
+__global__ void k_convert(Args a) {
+    size_t n = (size_t)a.n_real_total;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        long long v = (long long)a.qfix[k];
+        a.qfix[k] = 0ull;
+        a.qreal[k] = (float)((double)v * (1.0 / kFixScale));
+    }
+}
+
+void launch_convert(const Args& a, cudaStream_t s) {
+    int blocks = (int)((a.n_real_total + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_convert<<<blocks, 256, 0, s>>>(a);
+}
+
+// reciprocal-space convolution on the half spectrum; energies per CTA
+constexpr int kConvThreads = 256;
+__global__ void __launch_bounds__(kConvThreads) k_conv(Args a) {
+    __shared__ double red[2][kConvThreads];
+    int c = blockIdx.x;
+    const RepDev& R = a.reps[a.conv_cta_rep[c]];
+    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
+    const int Kzh = Kz / 2 + 1;
+    const long long nc = (long long)Kx * Ky * Kzh;
+    long long first = a.conv_cta_first[2 * c];
+    long long last = a.conv_cta_first[2 * c + 1];
+    float2* A = a.qcplx + R.cplx_off;
+    float2* B = A + nc;
+    const float* mx = a.moduli + R.mod_off[0];
+    const float* my = a.moduli + R.mod_off[1];
+    const float* mz = a.moduli + R.mod_off[2];
+    const float pi = 3.14159265358979f;
+    const float vol = R.box[0] * R.box[1] * R.box[2];
+    const float pref = 1.0f / (pi * vol);
+    const float fac = pi * pi / (a.alpha * a.alpha);
+    float ea = 0.f, eb = 0.f;
+    for (long long k = first + threadIdx.x; k < last; k += kConvThreads) {
+        int iz = (int)(k % Kzh);
+        long long rem = k / Kzh;
+        int iy = (int)(rem % Ky);
+        int ix = (int)(rem / Ky);
+        int mxi = ix <= Kx / 2 ? ix : ix - Kx;
+        int myi = iy <= Ky / 2 ? iy : iy - Ky;
+        float kx = mxi * R.ibox[0], ky = myi * R.ibox[1], kz = iz * R.ibox[2];
+        float m2 = kx * kx + ky * ky + kz * kz;
+        float G = (k == 0) ? 0.0f : pref * expf(-fac * m2) / (m2 * mx[ix] * my[iy] * mz[iz]);
+        float wgt = (iz == 0 || 2 * iz == Kz) ? 1.0f : 2.0f;
+        float2 qa = A[k], qb = B[k];
+        float na = qa.x * qa.x + qa.y * qa.y;
+        ea += 0.5f * wgt * G * na;
+        if (a.full) {
+            eb += 0.5f * wgt * G * (qb.x * qb.x + qb.y * qb.y);
+        } else {
+            eb += wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y));
+        }
+        A[k] = make_float2(G * qa.x, G * qa.y);
+        B[k] = make_float2(G * qb.x, G * qb.y);
+    }
+    red[0][threadIdx.x] = ea;
+    red[1][threadIdx.x] = eb;
+    __syncthreads();
+    for (int o = kConvThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 2) a.e_part_conv[2 * c + threadIdx.x] = red[threadIdx.x][0];
+}
+
+void launch_conv(const Args& a, cudaStream_t s) {
+    k_conv<<<a.conv_ctas, kConvThreads, 0, s>>>(a);
+}
+
+__device__ __forceinline__ void gather_one(const float* G, const RepDev& R, const Stencil& S, float& gx, float& gy,
+                                           float& gz) {
+    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
+    int iz[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        int v = S.base[2] - c;
+        iz[c] = v < 0 ? v + Kz : v;
+    }
+    gx = gy = gz = 0.f;
+#pragma unroll
+    for (int a0 = 0; a0 < 5; a0++) {
+        int ix = S.base[0] - a0;
+        if (ix < 0) ix += Kx;
+#pragma unroll
+        for (int b0 = 0; b0 < 5; b0++) {
+            int iy = S.base[1] - b0;
+            if (iy < 0) iy += Ky;
+            const float* rowp = G + ((size_t)ix * Ky + iy) * Kz;
+            float sx = 0.f, sz = 0.f;
+#pragma unroll
+            for (int c0 = 0; c0 < 5; c0++) {
+                float v = __ldg(rowp + iz[c0]);
+                sx += S.w[2][c0] * v;
+                sz += S.dw[2][c0] * v;
+            }
+            gx += S.dw[0][a0] * S.w[1][b0] * sx;
+            gy += S.w[0][a0] * S.dw[1][b0] * sx;
+            gz += S.w[0][a0] * S.w[1][b0] * sz;
+        }
+    }
+}
+
+__global__ void k_gather(Args a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.NA) return;
+    int b = s >> 5;
+    const RepDev& R = a.reps[a.block_rep[b]];
+    float4 p = a.posq[s];
+    if (p.w == 0.0f) return;
+    size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    const float* phi1 = a.qreal + R.real_off;
+    const float* phi2 = phi1 + G3;
+    const float sx = (float)R.K[0] * R.ibox[0], sy = (float)R.K[1] * R.ibox[1], sz = (float)R.K[2] * R.ibox[2];
+    Stencil S;
+    make_stencil(p.x, p.y, p.z, R, S, true);
+    float gx, gy, gz;
+    gather_one(phi1, R, S, gx, gy, gz);
+    float q = p.w;
+    fix_add(a.F + s, -q * gx * sx);
+    fix_add(a.F + a.NA + s, -q * gy * sy);
+    fix_add(a.F + 2 * (size_t)a.NA + s, -q * gz * sz);
+    unsigned long long* F2 = a.F + 3 * (size_t)a.NA;
+    if (a.full) {
+        float4 p2 = a.posq2[s];
+        make_stencil(p2.x, p2.y, p2.z, R, S, true);
+        gather_one(phi2, R, S, gx, gy, gz);
+        fix_add(F2 + s, -q * gx * sx);
+        fix_add(F2 + a.NA + s, -q * gy * sy);
+        fix_add(F2 + 2 * (size_t)a.NA + s, -q * gz * sz);
+    } else if (a.block_cls[b] == 0) {
+        // F2 - F1 of an atom that does not move: the potential of the moved charges
+        gather_one(phi2, R, S, gx, gy, gz);
+        fix_add(F2 + s, -q * gx * sx);
+        fix_add(F2 + a.NA + s, -q * gy * sy);
+        fix_add(F2 + 2 * (size_t)a.NA + s, -q * gz * sz);
+    } else {
+        // moving atom: F2 at x+d in phi1+dphi, minus F1 at x in phi1
+        float hx, hy, hz;
+        float4 d = a.displ[s];
+        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
+                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
+        gather_one(phi1, R, S, hx, hy, hz);
+        float kx, ky, kz;
+        gather_one(phi2, R, S, kx, ky, kz);
+        fix_add(F2 + s, -q * (hx + kx - gx) * sx);
+        fix_add(F2 + a.NA + s, -q * (hy + ky - gy) * sy);
+        fix_add(F2 + 2 * (size_t)a.NA + s, -q * (hz + kz - gz) * sz);
+    }
+}
+
+void launch_gather(const Args& a, cudaStream_t s) {
+    k_gather<<<(a.NA + 127) / 128, 128, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// finalize: one CTA per replica, FP64
+// ---------------------------------------------------------------------------
+
+// SoftCoreF of ReferenceATMMetaForceKernels.cpp:26-37
+__device__ double softcore(double u, double umax, double acore, double ub, double& fp) {
+    if (u <= ub) {
+        fp = 1.0;
+        return u;
+    }
+    double gu = (u - ub) / (acore * (umax - ub));
+    double zeta = 1.0 + 2.0 * gu * (gu + 1.0);
+    double zetap = pow(zeta, acore);
+    double sf = 4.0 * (2.0 * gu + 1.0) / zeta;
+    fp = sf * zetap / ((1.0 + zetap) * (1.0 + zetap));
+    return (umax - ub) * (zetap - 1.0) / (zetap + 1.0) + ub;
+}
+
+// The merge of ReferenceATMMetaForceKernels.cpp:82-98 plus the closed-form
+// parameter derivatives of W.
+__device__ void atm_merge(double E1, double E2, const double* p, double* out) {
+    double l1 = p[0], l2 = p[1], alpha = p[2], u0 = p[3], w0 = p[4];
+    double umax = p[5], ub = p[6], acore = p[7], dir = p[8];
+    double u = dir > 0 ? E2 - E1 : E1 - E2;
+    double e0 = dir > 0 ? E1 : E2;
+    double fp;
+    double usc = softcore(u, umax, acore, ub, fp);
+    double x = exp(-alpha * (usc - u0));
+    double ee = 1.0 + x;
+    double W = 0.0;
+    double L = log(ee);
+    if (alpha > 0) W = ((l2 - l1) / alpha) * L;
+    W += l2 * usc + w0;
+    double bfp = (l2 - l1) / ee + l1;
+    out[RES_ENERGY] = e0 + W;
+    out[RES_PERT] = usc;
+    out[RES_SP] = bfp * fp;
+    out[RES_W] = W;
+    out[RES_U] = u;
+    out[RES_E0] = e0;
+    out[RES_BFP] = bfp;
+    out[RES_FP] = fp;
+    out[RES_E1] = E1;
+    out[RES_E2] = E2;
+    if (alpha > 0) {
+        out[RES_DL1] = -L / alpha;
+        out[RES_DL2] = L / alpha + usc;
+        out[RES_DALPHA] = -(l2 - l1) / (alpha * alpha) * L - (l2 - l1) / alpha * (usc - u0) * x / ee;
+        out[RES_DU0] = (l2 - l1) * x / ee;
+    } else {
+        out[RES_DL1] = 0.0;
+        out[RES_DL2] = usc;
+        out[RES_DALPHA] = 0.0;
+        out[RES_DU0] = 0.0;
+    }
+    out[RES_DW0] = 1.0;
+}
+
+__device__ double block_sum(double v, double* sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ double rows_sum(const Args& a, int rb, int re) {
+    double s = 0.0;
+    for (int row = rb + threadIdx.x; row < re; row += blockDim.x) {
+        int n = a.row_count[row];
+        const double* e = a.e_tile + (size_t)row * a.row_cap;
+        for (int k = 0; k < n; k++) s += e[k];
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(256) k_finalize(Args a) {
+    __shared__ double sh[256];
+    int r = blockIdx.x;
+    const RepDev& R = a.reps[r];
+    double dir1 = block_sum(rows_sum(a, R.row1_b, R.row1_e), sh);
+    double dir2 = block_sum(rows_sum(a, R.row2_b, R.row2_e), sh);
+    double x1 = 0, x2 = 0, xd = 0, c1 = 0, c2 = 0;
+    for (int c = R.exc_cta_b + threadIdx.x; c < R.exc_cta_e; c += blockDim.x) {
+        x1 += a.e_part_exc[3 * c];
+        x2 += a.e_part_exc[3 * c + 1];
+        xd += a.e_part_exc[3 * c + 2];
+    }
+    for (int c = R.conv_cta_b + threadIdx.x; c < R.conv_cta_e; c += blockDim.x) {
+        c1 += a.e_part_conv[2 * c];
+        c2 += a.e_part_conv[2 * c + 1];
+    }
+    x1 = block_sum(x1, sh);
+    x2 = block_sum(x2, sh);
+    xd = block_sum(xd, sh);
+    c1 = block_sum(c1, sh);
+    c2 = block_sum(c2, sh);
+    if (threadIdx.x == 0) {
+        double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
+        double E2;
+        if (a.full) {
+            E2 = dir2 + x2 + c2 + R.e_self + R.e_disp;
+        } else {
+            E2 = E1 + (dir2 + xd + c2);
+        }
+        double* out = a.results + (size_t)r * NUM_RES;
+        // a NonbondedForce outside the variable groups contributes nothing to U_var
+        atm_merge(R.var_nb ? E1 : 0.0, R.var_nb ? E2 : 0.0, R.params, out);
+        out[RES_E1] = E1;  // the NonbondedForce energy at x and at x + d
+        out[RES_E2] = E2;
+        out[RES_STATUS] = (double)a.status->overflow;
+    }
+}
+
+void launch_finalize(const Args& a, cudaStream_t s) {
+    k_finalize<<<a.R, 256, 0, s>>>(a);
+}
+
+// hybrid forces in user order
+__global__ void k_output(Args a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.NA) return;
+    int o = a.orig[s];
+    if (o < 0) return;
+    int rep = a.block_rep[s >> 5];
+    const RepDev& R = a.reps[rep];
+    const double* res = a.results + (size_t)rep * NUM_RES;
+    double sp = res[RES_SP];
+    double w = R.params[8] > 0 ? sp : 1.0 - sp;
+    size_t out = 3 * (size_t)(R.in_off + o);
+    for (int k = 0; k < 3; k++) {
+        long long f1 = (long long)a.F[(size_t)k * a.NA + s];
+        long long f2 = (long long)a.F[(size_t)(3 + k) * a.NA + s];
+        double d = a.full ? (double)(f2 - f1) : (double)f2;
+        double f = R.var_nb ? ((double)f1 + w * d) * (1.0 / kFixScale) : 0.0;
+        a.f_out[out + k] = f;
+        if (a.f_nb) a.f_nb[out + k] = (double)f1 * (1.0 / kFixScale);
+    }
+}
+
+void launch_output(const Args& a, cudaStream_t s) {
+    k_output<<<(a.NA + 255) / 256, 256, 0, s>>>(a);
+}
+
+// replicas x states energy matrix: beta * (e0(r; dir_s) + W_s(usc_s(u(r; dir_s))))
+__global__ void k_matrix(Args a) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.R * a.R) return;
+    int r = idx / a.R, s = idx % a.R;
+    const double* res = a.results + (size_t)r * NUM_RES;
+    double out[NUM_RES];
+    bool v = a.reps[r].var_nb;
+    atm_merge(v ? res[RES_E1] : 0.0, v ? res[RES_E2] : 0.0, a.reps[s].params, out);
+    a.matrix[idx] = *a.beta * out[RES_ENERGY];
+}
+
+void launch_matrix(const Args& a, cudaStream_t s) {
+    int n = a.R * a.R;
+    k_matrix<<<(n + 127) / 128, 128, 0, s>>>(a);
+}
+
+}  // namespace atm

@@ -1,0 +1,151 @@
+// Device data layout and kernel interfaces of the ATM evaluation engine.
+//
+// Atoms of all replicas live in one "slot" space: each replica's atoms are
+// reordered (non-moving molecules along a Hilbert curve, then each displacement
+// class) and padded so that every 32-slot block belongs to one replica and one
+// displacement class.  Forces accumulate as 64-bit fixed point (2^32 units per
+// kJ/mol/nm) so that sums are exact and independent of launch order; energies
+// are summed in FP64 through per-tile / per-CTA partials in fixed order.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace atm {
+
+constexpr int kTile = 32;
+constexpr double kFixScale = 4294967296.0;  // 2^32
+constexpr float kFixScaleF = 4294967296.0f;
+constexpr int kOrder = 5;  // PME B-spline order (OpenMM's)
+
+// Row kinds of the pair-tile lists.
+enum RowKind { ROW_STATE1 = 0, ROW_STATE2 = 1, ROW_DIFF1 = 2, ROW_DIFF2 = 3 };
+
+// Result record layout (matches ATM_RES_* in include/atm_capi.h).
+enum Res {
+    RES_ENERGY = 0, RES_PERT, RES_SP, RES_W, RES_U, RES_E0, RES_BFP, RES_FP, RES_E1, RES_E2,
+    RES_DL1, RES_DL2, RES_DALPHA, RES_DU0, RES_DW0, RES_STATUS, NUM_RES
+};
+
+// Per-replica constants and offsets (device copy refreshed every evaluation).
+struct RepDev {
+    float box[4];      // L (x,y,z), unused
+    float ibox[4];     // 1/L
+    double boxd[3];
+    int slot_begin, slot_end;
+    int block_begin, block_end;
+    int mov_block_begin;      // first moving block (== block_end when none)
+    int in_off;               // first atom of this replica in user-order arrays
+    int n;                    // atoms (user order)
+    int K[3];                 // PME grid
+    int mod_off[3];           // offsets of the B-spline moduli (per dimension)
+    long long real_off;       // first float of this replica's two real grids
+    long long cplx_off;       // first complex of its two spectra
+    long long fixed_off;      // first int64 of its two fixed-point charge grids
+    int row1_b, row1_e;       // rows of state 1 (full and difference modes)
+    int row2_b, row2_e;       // rows of state 2 (full) or of the difference tiles (diff)
+    int exc_cta_b, exc_cta_e; // exception-kernel CTAs (energy partials)
+    int conv_cta_b, conv_cta_e;
+    int var_nb;               // the NonbondedForce is in the ATM variable groups
+    int pad0;
+    double e_self;            // PME self energy (FP64, host)
+    double e_disp;            // dispersion correction (FP64, host)
+    double params[9];         // ATM globals
+};
+
+// Parameters of one exception pair (x: chargeProd * ke, y: sigma, z: epsilon,
+// w: ke * q_i * q_j for the Ewald exclusion correction).
+struct __align__(16) ExcParam {
+    double x, y, z, w;
+};
+
+struct Status {
+    int tile_count;   // tiles appended by the finder
+    int overflow;     // bit 0: tile list, bit 1: row capacity
+    int max_row;      // largest row seen
+    int pad;
+};
+
+// Arguments shared by the kernels of one engine (passed by value).
+struct Args {
+    // sizes
+    int R, NA, NB, nrows, row_cap, tile_cap, n_in;
+    int full;                 // 1: two full states, 0: state 1 + difference
+    // method
+    int method;               // 2 reaction field, 4 PME
+    float rc2, alpha, krf, crf;
+    double alphad, cutoffd;
+    // replicas
+    RepDev* reps;
+    // user-order inputs and outputs
+    const double* pos_in;     // 3*n_in
+    const double* displ_in;   // 3*n_in
+    const int* slot_of;       // n_in
+    double* f_out;            // 3*n_in (ATM force)
+    double* f_nb;             // 3*n_in (state-1 nonbonded force) or null
+    // slot arrays
+    const int* orig;          // NA: user index within the replica, -1 for padding
+    const float* qs;          // NA: charge * sqrt(1/(4 pi eps0))
+    const float2* lj;         // NA: (sigma/2, 2 sqrt(eps))
+    const float4* displ;      // NA: displacement (sorted)
+    float4* posq;             // NA: wrapped positions + scaled charge (state 1)
+    float4* posq2;            // NA: state 2 (full mode) or null
+    // blocks
+    const int* block_rep;     // NB
+    const int* block_cls;     // NB: displacement class (0 = not moving)
+    const float4* block_d;    // NB: displacement of the block's class
+    float4* bb_c;             // NB: bounding-box centres (state 1)
+    float4* bb_h;             // NB: half extents
+    float4* bb_c2;            // NB: state 2 (full mode)
+    float4* bb_h2;
+    // rows and tiles
+    const int4* row_desc;     // nrows: (I, kind, replica, 0)
+    int* row_count;           // nrows
+    const int* ex_start;      // NB+1: exclusion tiles of row I (regular rows)
+    const int2* ex_ent;       //   (J, mask id)
+    const int* dx_start;      // NB+1: cross-class exclusion tiles (difference rows)
+    const int2* dx_ent;
+    const uint32_t* masks;    // 32 words per mask
+    int4* tiles;              // tile_cap: (I, J, row | kind<<28, (mask+1) | slot<<20)
+    double* e_tile;           // nrows*row_cap
+    Status* status;
+    // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]
+    unsigned long long* F;
+    // exceptions (user-order indices, grouped by replica)
+    int n_exc;
+    const int4* exc_ij;       // (i_in, j_in, replica, cross)
+    const ExcParam* exc_p;    // (chargeProd*ke, sigma, epsilon, q_i q_j ke)
+    double* e_part_exc;       // 3 per CTA: state 1, state 2, difference
+    int exc_ctas;
+    const int* exc_cta_first; // first exception of each CTA
+    // PME
+    unsigned long long* qfix; // fixed-point charge grids
+    float* qreal;             // real grids (charge, then potential)
+    float2* qcplx;            // spectra
+    const float* moduli;      // B-spline moduli, per replica per dimension
+    double* e_part_conv;      // 2 per CTA
+    int conv_ctas;
+    const int* conv_cta_rep;  // replica of each conv CTA
+    const long long* conv_cta_first;  // first complex element of each conv CTA
+    long long n_real_total;
+    // results
+    double* results;          // R * NUM_RES
+    double* matrix;           // R * R
+    const double* beta;       // device scalar
+};
+
+void launch_prepare(const Args& a, cudaStream_t s);
+void launch_find(const Args& a, cudaStream_t s);
+void launch_tiles(const Args& a, int grid, cudaStream_t s);
+void launch_exceptions(const Args& a, cudaStream_t s);
+void launch_spread(const Args& a, cudaStream_t s);
+void launch_convert(const Args& a, cudaStream_t s);
+void launch_conv(const Args& a, cudaStream_t s);
+void launch_gather(const Args& a, cudaStream_t s);
+void launch_finalize(const Args& a, cudaStream_t s);
+void launch_output(const Args& a, cudaStream_t s);
+void launch_matrix(const Args& a, cudaStream_t s);
+int tiles_kernel_blocks_per_sm();
+constexpr int kTileThreads = 256;
+
+}  // namespace atm

@@ -1,0 +1,224 @@
+"""Parity of the CUDA path with the FP64 oracle, through the C ABI.
+
+Tolerances (BASELINE the benchmark spec): perturbation energy u within 0.01 kJ/mol,
+force RMS relative error <= 1e-4.  Total energies, which the reference gives in
+double precision, are compared with a relative tolerance of 2e-6 of the sum of
+the magnitudes of the energy terms (FP32 pair arithmetic).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import atmmetaforce as atm
+import oracle as O
+from atmmetaforce import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+U_TOL = 0.01
+F_TOL = 1e-4
+
+
+def _has_gpu():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+if not _has_gpu():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _threads():
+    O.set_threads(min(16, os.cpu_count() or 1))
+    yield
+    O.set_threads(1)
+
+
+def force_rel(F, G):
+    return float(np.sqrt(((F - G) ** 2).sum() / (G ** 2).sum()))
+
+
+def energy_tol(spec, pos):
+    _, _, T = O.nonbonded(spec, pos, forces=False)
+    return 2e-6 * (sum(abs(v) for v in T.values()) + 1.0)
+
+
+def run_context(case, diff, groups=(2,)):
+    sys_, nb, f = atm.system_from_case(case)
+    ctx = atm.Context(sys_, 0, {"DifferencePath": int(diff)})
+    ctx.setPositions(case.pos)
+    st = ctx.getState(getEnergy=True, getForces=True, groups=set(groups))
+    return ctx, f, st
+
+
+def check_case(case, diff):
+    ctx, f, st = run_context(case, diff)
+    ref = O.atm_eval(case.spec, case.pos, case.displ, case.params)
+    u = f.getPerturbationEnergy(ctx)
+    assert abs(u - ref["usc"]) <= U_TOL, (u, ref["usc"])
+    assert force_rel(st.getForces(), ref["forces"]) <= F_TOL
+    tol = energy_tol(case.spec, case.pos)
+    assert abs(st.getPotentialEnergy() - ref["energy"]) <= tol, (st.getPotentialEnergy(), ref["energy"], tol)
+    r = st.getResults()
+    assert r["status"] == 0
+    assert abs(r["sp"] - ref["sp"]) <= 1e-6 * max(1.0, abs(ref["sp"]))
+    return ctx, f, st, ref
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_reaction_field_2394(diff):
+    check_case(S.abfe_rf_2394(0), diff)
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_pme_small(diff):
+    c = S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=11,
+                           params=S.default_params(0.2, 0.7, 0.1, 30.0, 2.0))
+    check_case(c, diff)
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_pme_23558(diff):
+    check_case(S.abfe_pme_23558(1), diff)
+
+
+def test_deterministic_bitwise():
+    c = S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=12)
+    sys_, nb, f = atm.system_from_case(c)
+    ctx = atm.Context(sys_, 0, {"DifferencePath": 1})
+    ctx.setPositions(c.pos)
+    a = ctx.getState(getEnergy=True, getForces=True, groups={2})
+    ctx.setPositions(c.pos)  # forces a second evaluation
+    b = ctx.getState(getEnergy=True, getForces=True, groups={2})
+    assert np.array_equal(a.getForces(), b.getForces())
+    assert a.getPotentialEnergy() == b.getPotentialEnergy()
+
+
+def test_batch_mixed_sizes_vs_oracle_and_matrix():
+    cases = [S.abfe_pme_small(1500, 8, 21), S.abfe_pme_small(4000, 18, 22),
+             S.abfe_pme_small(2500, 12, 23, displ=1.2), S.abfe_pme_small(6000, 30, 24)]
+    for k, c in enumerate(cases):
+        l1, l2 = S.SCHEDULE_22[5 * k]
+        c.params = S.default_params(l1, l2, 0.1, 110.0 - 40 * k, 0.5 * k, 200.0, 100.0, 0.0625, 1.0 if k != 2 else -1.0)
+    systems = [atm.system_from_case(c)[0] for c in cases]
+    b = atm.ReplicaBatch(systems, 0)
+    pos = np.concatenate([c.pos for c in cases])
+    E, F, res = b.evaluate(pos)
+    refs = []
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        refs.append(ref)
+        assert abs(res[k]["pert"] - ref["usc"]) <= U_TOL
+        Fk = F[b.offsets[k]:b.offsets[k + 1]]
+        assert force_rel(Fk, ref["forces"]) <= F_TOL
+        assert abs(E[k] - ref["energy"]) <= energy_tol(c.spec, c.pos)
+    M = b.energyMatrix(beta=0.4)
+    for r in range(len(cases)):
+        for s in range(len(cases)):
+            m = O.atm_merge(refs[r]["E1"], refs[r]["E2"], cases[s].params)
+            tol = 0.4 * (energy_tol(cases[r].spec, cases[r].pos) + U_TOL)
+            assert abs(M[r, s] - 0.4 * m["energy"]) <= tol
+
+
+def test_batch_matches_single_contexts():
+    cases = [S.abfe_pme_small(2000, 10, 31), S.abfe_pme_small(2000, 10, 32)]
+    systems = [atm.system_from_case(c)[0] for c in cases]
+    b = atm.ReplicaBatch(systems, 0)
+    E, F, res = b.evaluate(np.concatenate([c.pos for c in cases]))
+    for k, c in enumerate(cases):
+        ctx, f, st = run_context(c, 1)
+        np.testing.assert_allclose(F[b.offsets[k]:b.offsets[k + 1]], st.getForces(), rtol=0, atol=1e-6)
+        assert abs(res[k]["pert"] - f.getPerturbationEnergy(ctx)) < 1e-6
+
+
+def test_temoa_g1_reference_pin_on_gpu():
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "temoa_g1.npz"))
+    alpha, grid = S.pme_parameters(float(z["cutoff"]), float(z["ewald_tol"]), z["box_default"])
+    spec = S.NonbondedSpec(charge=z["charge"], sigma=z["sigma"], epsilon=z["epsilon"], exc_i=z["exc_i"],
+                           exc_j=z["exc_j"], exc_qq=z["exc_qq"], exc_sig=z["exc_sig"], exc_eps=z["exc_eps"],
+                           method=S.PME, cutoff=float(z["cutoff"]), box=z["box"], alpha=alpha, grid=tuple(grid),
+                           use_disp_corr=True)
+    d = np.zeros_like(z["pos"])
+    d[z["ligand"]] = z["displacement"]
+    case = S.ATMCase(spec=spec, pos=z["pos"], displ=d, params=z["params"])
+    for diff in (0, 1):
+        ctx, f, st = run_context(case, diff)
+        u = f.getPerturbationEnergy(ctx)
+        # python/tests/test_abfe.py:148,150
+        assert abs(u - float(z["expected_u"])) <= float(z["expected_u_atol"]), u
+        ref = O.atm_eval(spec, z["pos"], d, z["params"])
+        assert abs(u - ref["usc"]) <= U_TOL
+        assert force_rel(st.getForces(), ref["forces"]) <= F_TOL
+
+
+def test_parameters_softcore_direction_and_alpha_zero():
+    c = S.water_ligand_box(2500, 3.0, [14], [(1.3, 1.4, 1.2)], S.PME, 0.9, seed=41)
+    sys_, nb, f = atm.system_from_case(c)
+    ctx = atm.Context(sys_, 0, {"DifferencePath": 1})
+    ctx.setPositions(c.pos)
+    E1 = O.nonbonded(c.spec, c.pos, forces=False)[0]
+    E2 = O.nonbonded(c.spec, c.pos + c.displ, forces=False)[0]
+    u = E2 - E1
+    settings = [
+        dict(ATMDirection=-1.0),
+        dict(ATMDirection=1.0, ATMUbcore=u - 20.0, ATMUmax=u + 50.0, ATMAcore=0.0625),  # soft-core active
+        dict(ATMAlpha=0.0, ATMLambda1=0.2, ATMLambda2=0.6),  # alpha = 0 quirk
+        dict(ATMAlpha=0.3, ATMU0=u, ATMW0=3.0),
+    ]
+    p = c.params.copy()
+    for st_ in settings:
+        for k, v in st_.items():
+            ctx.setParameter(k, v)
+            p[S.PARAM_NAMES.index(k)] = v
+        s = ctx.getState(getEnergy=True, getForces=True, groups={2})
+        ref = O.atm_merge(E1, E2, p)
+        assert abs(f.getPerturbationEnergy(ctx) - ref["usc"]) <= U_TOL
+        assert abs(s.getResults()["sp"] - ref["sp"]) <= 1e-5
+        assert abs(ctx.getParameter(list(st_)[0]) - list(st_.values())[0]) == 0
+
+
+def test_group_semantics_and_nonbonded_group():
+    c = S.water_ligand_box(1500, 2.5, [10], [(1.2, 1.2, 1.2)], S.PME, 0.9, seed=51)
+    sys_, nb, f = atm.system_from_case(c)
+    ctx = atm.Context(sys_, 0)
+    ctx.setPositions(c.pos)
+    # only the NonbondedForce's group: its state-1 energy and forces
+    s1 = ctx.getState(getEnergy=True, getForces=True, groups={1})
+    E1, F1, _ = O.nonbonded(c.spec, c.pos)
+    assert abs(s1.getPotentialEnergy() - E1) <= energy_tol(c.spec, c.pos)
+    assert force_rel(s1.getForces(), F1) <= F_TOL
+    # the ATM group not requested: perturbation energy not refreshed (ATMMetaForceImpl.cpp:148)
+    assert f.getPerturbationEnergy(ctx) == 0.0
+    ctx.getState(getEnergy=True, groups={2})
+    assert f.getPerturbationEnergy(ctx) != 0.0
+
+
+def test_update_parameters_in_context_and_no_moving_atoms():
+    c = S.water_ligand_box(1500, 2.5, [10], [(1.2, 1.2, 1.2)], S.PME, 0.9, seed=61)
+    sys_, nb, f = atm.system_from_case(c)
+    ctx = atm.Context(sys_, 0, {"DifferencePath": 1})
+    ctx.setPositions(c.pos)
+    ctx.getState(getEnergy=True, groups={2})
+    lig = c.ligands[0]
+    d2 = c.displ.copy()
+    d2[lig] = (1.0, -1.1, 0.9)
+    for i in lig:
+        f.setParticleParameters(int(i), int(i), *d2[i])
+    f.updateParametersInContext(ctx)
+    ctx.getState(getEnergy=True, groups={2})
+    ref = O.atm_eval(c.spec, c.pos, d2, c.params)
+    assert abs(f.getPerturbationEnergy(ctx) - ref["usc"]) <= U_TOL
+    # no displacement at all: u = 0 exactly and the ATM force is the state-1 force
+    for i in lig:
+        f.setParticleParameters(int(i), int(i), 0.0, 0.0, 0.0)
+    f.updateParametersInContext(ctx)
+    s = ctx.getState(getEnergy=True, getForces=True, groups={2})
+    assert f.getPerturbationEnergy(ctx) == 0.0
+    E1, F1, _ = O.nonbonded(c.spec, c.pos)
+    assert force_rel(s.getForces(), F1) <= F_TOL
