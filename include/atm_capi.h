@@ -198,6 +198,29 @@ int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_
  * replica s's alchemical parameters, from the last evaluation. */
 int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix);
 
+/* ---- allocation-free variant ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * code whose device memory all comes from its own pool or arena, or that runs
+ * where new allocations are forbidden (a budget already handed out, an
+ * allocator that must not be re-entered, a step that must not pay allocation
+ * latency).  Reaction-field (CutoffPeriodic) NonbondedForce energy and forces
+ * of n <= 16384 particles, every pair within the cutoff except the excluded
+ * ones, on the current device and the given stream.  All pointers except box
+ * are device pointers the caller owns: d_pos (n x 3 nm), d_charge, d_sigma,
+ * d_epsilon (n each), excluded partners as CSR (d_excl_start[n+1], d_excl,
+ * both directions listed), outputs d_energy (1, kJ/mol) and d_forces (n x 3,
+ * kJ/mol/nm); box = 3 host doubles (orthorhombic edges, each >= 2 cutoff).
+ * It allocates nothing: its scratch (about 400 KB of fixed-point force
+ * accumulators and energy partials) is a static device array that every GPU
+ * loading the library holds until exit, cleared at the start of every call.
+ * The first call on a device looks up that array's address; make that first
+ * call before any stream capture.  Calls that overlap on the GPU (other
+ * streams, other threads) share the array and race.  Larger n returns
+ * ATM_ERR_INVALID_ARGUMENT. */
+int atm_rf_nonbonded_noalloc(int n, const double* d_pos, const double* d_charge, const double* d_sigma,
+                             const double* d_epsilon, const int* d_excl_start, const int* d_excl, const double* box,
+                             double cutoff, double eps_rf, double* d_energy, double* d_forces, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Timings (ms) of the kernels of the last evaluate() when profiling is on. */
 int atm_batch_set_profiling(atm_batch_t b, int on);

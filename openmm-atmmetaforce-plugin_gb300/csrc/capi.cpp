@@ -51,6 +51,10 @@ struct atm_batch_s {
 
 static thread_local std::string g_error;
 
+namespace atm {
+void set_last_error(const std::string& msg) { g_error = msg; }
+}  // namespace atm
+
 #define API_BEGIN try {
 #define API_END                                    \
     g_error.clear();                               \
