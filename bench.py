@@ -312,7 +312,8 @@ def main():
                 "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
-                "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt}
+                "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt, "tile_stats": batch.stats(),
+                "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 1024 * batch.stats()["tiles"])}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

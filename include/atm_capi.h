@@ -227,6 +227,8 @@ int atm_batch_set_profiling(atm_batch_t b, int on);
 int atm_batch_get_kernel_times(atm_batch_t b, char* names, size_t names_cap, double* ms, int cap, int* n);
 /* Number of the library's own kernel launches per evaluation. */
 int atm_batch_get_launch_count(atm_batch_t b, int* n);
+/* Pair tiles of the last evaluation, tile rows, and the largest row (nullable outputs). */
+int atm_batch_get_stats(atm_batch_t b, int* tiles, int* rows, int* max_row);
 
 #ifdef __cplusplus
 }

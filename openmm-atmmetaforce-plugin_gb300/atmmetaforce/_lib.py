@@ -100,6 +100,7 @@ _SIGS = {
     "atm_batch_set_profiling": [_vp, C.c_int],
     "atm_batch_get_kernel_times": [_vp, C.c_char_p, _sz, _dp, C.c_int, _ip],
     "atm_batch_get_launch_count": [_vp, _ip],
+    "atm_batch_get_stats": [_vp, _ip, _ip, _ip],
     "atm_rf_nonbonded_noalloc": [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _dp, C.c_double, C.c_double, _vp, _vp,
                                  _vp],
 }

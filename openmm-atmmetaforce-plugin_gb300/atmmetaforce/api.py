@@ -489,3 +489,9 @@ class ReplicaBatch:
         n = C.c_int()
         call("atm_batch_get_launch_count", self._h, C.byref(n))
         return n.value
+
+    def stats(self):
+        """Pair tiles of the last evaluation, tile rows and the largest row."""
+        t, r, m = C.c_int(), C.c_int(), C.c_int()
+        call("atm_batch_get_stats", self._h, C.byref(t), C.byref(r), C.byref(m))
+        return {"tiles": t.value, "rows": r.value, "max_row": m.value}

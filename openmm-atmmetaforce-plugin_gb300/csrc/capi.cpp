@@ -695,4 +695,11 @@ int atm_batch_get_launch_count(atm_batch_t b, int* n) {
     API_END
 }
 
+int atm_batch_get_stats(atm_batch_t b, int* tiles, int* rows, int* max_row) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    b->eng->stats(tiles, rows, max_row);
+    API_END
+}
+
 }  // extern "C"

@@ -587,7 +587,7 @@ void Engine::build_layout() {
         rep_host_[r].e_disp = 0.0;
         if (s.dispersion) rep_host_[r].e_disp = dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]);
     }
-    if (tile_cap_ == 0) tile_cap_ = nrows_ * 40 + 4096;
+    if (tile_cap_ == 0) tile_cap_ = nrows_ * 28 + 4096;
     layout_ready_ = true;
 }
 
@@ -669,6 +669,7 @@ void Engine::alloc_device() {
     a.dx_ent = dupload(d_allocs_, dx_ent_);
     a.masks = dupload(d_allocs_, masks_);
     a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
+    a.tile_j = dalloc<int>(d_allocs_, 32 * (size_t)tile_cap_);
     a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
     a.status = dalloc<Status>(d_allocs_, 1);
     a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);
@@ -788,6 +789,8 @@ void Engine::record(cudaStream_t st, bool host_io) {
 
 bool Engine::check_status_and_grow() {
     const Status& s = *h_status_;
+    last_tiles_ = s.tile_count;
+    last_max_row_ = s.max_row;
     if (!s.overflow) return false;
     if (s.overflow & 2) {
         int want = (int)(s.max_row * 1.25) + 8;

@@ -69,6 +69,12 @@ public:
     void set_profiling(bool on) { profiling_ = on; }
     const std::vector<KernelTime>& kernel_times() const { return times_; }
     int launches_per_eval() const;
+    // tiles of the last evaluation, tile rows, and the largest row
+    void stats(int* tiles, int* rows, int* max_row) const {
+        if (tiles) *tiles = last_tiles_;
+        if (rows) *rows = nrows_;
+        if (max_row) *max_row = last_max_row_;
+    }
 
 private:
     void build_layout();
@@ -90,6 +96,7 @@ private:
     int NA_ = 0, NB_ = 0, nrows_ = 0;
     int row_cap_ = 96;
     int tile_cap_ = 0;
+    int last_tiles_ = 0, last_max_row_ = 0;
     int method_ = 0;
     double cutoff_ = 1.0, alpha_ = 0.0, krf_ = 0.0, crf_ = 0.0;
     double beta_ = 1.0;

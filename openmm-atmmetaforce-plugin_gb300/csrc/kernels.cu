@@ -104,255 +104,7 @@ void launch_prepare(const Args& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // find: one warp per row; bounding-box test of block I against candidates J
 // ---------------------------------------------------------------------------
-constexpr int kFindWarps = 4;
-constexpr int kMaxRowCap = 1024;
-
-__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj, const RepDev& R, float rc2) {
-    float dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
-    dx -= R.box[0] * rintf(dx * R.ibox[0]);
-    dy -= R.box[1] * rintf(dy * R.ibox[1]);
-    dz -= R.box[2] * rintf(dz * R.ibox[2]);
-    dx = fmaxf(0.f, fabsf(dx) - hi.x - hj.x);
-    dy = fmaxf(0.f, fabsf(dy) - hi.y - hj.y);
-    dz = fmaxf(0.f, fabsf(dz) - hi.z - hj.z);
-    return dx * dx + dy * dy + dz * dz < rc2;
-}
-
-__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
-    __shared__ int2 stage[kFindWarps][kMaxRowCap];
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int row = blockIdx.x * kFindWarps + w;
-    if (row >= a.nrows) return;
-    int4 d = a.row_desc[row];
-    int I = d.x, kind = d.y, rep = d.z;
-    const RepDev& R = a.reps[rep];
-    int2* st = stage[w];
-    int cap = a.row_cap < kMaxRowCap ? a.row_cap : kMaxRowCap;
-    bool diff = kind >= ROW_DIFF1;
-    bool g2 = kind == ROW_DIFF2;
-    const int* es = diff ? a.dx_start : a.ex_start;
-    const int2* ee = diff ? a.dx_ent : a.ex_ent;
-    int e0 = es[I], e1 = es[I + 1];
-    int n = 0;
-    // exclusion tiles first (always processed)
-    for (int k = e0 + lane; k < e1; k += 32) {
-        int pos = k - e0;
-        if (pos < cap) st[pos] = ee[k];
-    }
-    n = e1 - e0;
-    float4 ci, hi;
-    if (kind == ROW_STATE2) {
-        ci = a.bb_c2[I];
-        hi = a.bb_h2[I];
-    } else {
-        ci = a.bb_c[I];
-        hi = a.bb_h[I];
-        if (g2) {
-            float4 dd = a.block_d[I];
-            ci.x += dd.x;
-            ci.y += dd.y;
-            ci.z += dd.z;
-        }
-    }
-    int cls_i = a.block_cls[I];
-    int jb = diff ? R.block_begin : I + 1;
-    int je = R.block_end;
-    for (int base = jb; base < je; base += 32) {
-        int J = base + lane;
-        bool ok = false;
-        if (J < je) {
-            if (diff) {
-                int cj = a.block_cls[J];
-                ok = (J != I) && cj != cls_i && (cj == 0 || cls_i < cj);
-            } else {
-                ok = true;
-            }
-            if (ok) {
-                float4 cj4, hj4;
-                if (kind == ROW_STATE2) {
-                    cj4 = a.bb_c2[J];
-                    hj4 = a.bb_h2[J];
-                } else {
-                    cj4 = a.bb_c[J];
-                    hj4 = a.bb_h[J];
-                    if (g2 && a.block_cls[J] != 0) {
-                        float4 dd = a.block_d[J];
-                        cj4.x += dd.x;
-                        cj4.y += dd.y;
-                        cj4.z += dd.z;
-                    }
-                }
-                ok = boxes_close(ci, hi, cj4, hj4, R, a.rc2);
-            }
-            if (ok) {
-                for (int k = e0; k < e1; k++)
-                    if (ee[k].x == J) ok = false;
-            }
-        }
-        unsigned bal = __ballot_sync(FULL_MASK, ok);
-        if (ok) {
-            int pos = n + __popc(bal & ((1u << lane) - 1u));
-            if (pos < cap) st[pos] = make_int2(J, -1);
-        }
-        n += __popc(bal);
-    }
-    __syncwarp();
-    if (n > cap) {
-        if (lane == 0) {
-            atomicOr(&a.status->overflow, 2);
-            atomicMax(&a.status->max_row, n);
-        }
-        n = cap;
-    }
-    int tbase = 0;
-    if (lane == 0) tbase = atomicAdd(&a.status->tile_count, n);
-    tbase = __shfl_sync(FULL_MASK, tbase, 0);
-    if (lane == 0) a.row_count[row] = n;
-    if (tbase + n > a.tile_cap) {
-        if (lane == 0) atomicOr(&a.status->overflow, 1);
-        return;
-    }
-    for (int k = lane; k < n; k += 32) {
-        int2 e = st[k];
-        a.tiles[tbase + k] = make_int4(I, e.x, row | (kind << 28), (e.y + 1) | (k << 20));
-    }
-}
-
-void launch_find(const Args& a, cudaStream_t s) {
-    int blocks = (a.nrows + kFindWarps - 1) / kFindWarps;
-    k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
-}
-
-// ---------------------------------------------------------------------------
-// tiles: persistent warps, static stride over the tile list
-// ---------------------------------------------------------------------------
-
-// erfc(x) for x >= 0: Abramowitz & Stegun, Handbook of Mathematical Functions,
-// eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term.
-__device__ __forceinline__ float erfc_as(float x, float expmx2) {
-    float t = 1.0f / (1.0f + 0.3275911f * x);
-    float p = t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
-    return p * expmx2;
-}
-
-template <int METHOD>
-__device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float eps4, float alpha, float krf, float crf,
-                                          float& e, float& fr) {
-    float invr = rsqrtf(r2);
-    float invr2 = invr * invr;
-    float s2 = sig * sig * invr2;
-    float s6 = s2 * s2 * s2;
-    e = eps4 * (s6 * s6 - s6);
-    fr = eps4 * (12.0f * s6 * s6 - 6.0f * s6) * invr2;
-    if (METHOD == 4) {
-        float r = r2 * invr;
-        float ar = alpha * r;
-        float ex = __expf(-ar * ar);
-        float ec = erfc_as(ar, ex);
-        e += qq * ec * invr;
-        fr += qq * (ec * invr + 1.1283791670955126f * alpha * ex) * invr2;
-    } else {
-        e += qq * (invr + krf * r2 - crf);
-        fr += qq * (invr * invr2 - 2.0f * krf);
-    }
-}
-
-template <int METHOD>
-__global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    int ntiles = a.status->tile_count;
-    if (ntiles > a.tile_cap) ntiles = a.tile_cap;
-    const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
-    for (int t = gw; t < ntiles; t += nw) {
-        const int4 T = a.tiles[t];
-        const int I = T.x, J = T.y;
-        const int row = T.z & 0x0fffffff, kind = (unsigned)T.z >> 28;
-        const int maskid = (T.w & 0xfffff) - 1, slot = (unsigned)T.w >> 20;
-        const int rep = a.block_rep[I];
-        const float Lx = a.reps[rep].box[0], Ly = a.reps[rep].box[1], Lz = a.reps[rep].box[2];
-        const float iLx = a.reps[rep].ibox[0], iLy = a.reps[rep].ibox[1], iLz = a.reps[rep].ibox[2];
-        const bool diff = kind >= ROW_DIFF1;
-        const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
-        const int i = I * kTile + lane;
-        const int j0 = J * kTile + lane;
-        float4 pi = P[i];
-        float4 pj = P[j0];
-        const float2 li = a.lj[i];
-        float2 lj = a.lj[j0];
-        if (kind == ROW_DIFF2) {
-            float4 di = a.displ[i], dj = a.displ[j0];
-            pi.x += di.x; pi.y += di.y; pi.z += di.z;
-            pj.x += dj.x; pj.y += dj.y; pj.z += dj.z;
-        }
-        const unsigned mask = maskid >= 0 ? a.masks[(size_t)maskid * 32 + lane] : FULL_MASK;
-        const bool diag = (I == J);
-        float fix = 0.f, fiy = 0.f, fiz = 0.f, fjx = 0.f, fjy = 0.f, fjz = 0.f;
-        float e32 = 0.f;
-        double e64 = 0.0;
-        const int src = (lane + 1) & 31;
-#pragma unroll 4
-        for (int k = 0; k < 32; k++) {
-            float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-            dx -= Lx * rintf(dx * iLx);
-            dy -= Ly * rintf(dy * iLy);
-            dz -= Lz * rintf(dz * iLz);
-            float r2 = dx * dx + dy * dy + dz * dz;
-            if (((mask >> k) & 1u) && r2 < rc2) {
-                float e, fr;
-                pair_eval<METHOD>(r2, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
-                if (diff) e64 += (double)e;
-                else e32 += e;
-                float fx = fr * dx, fy = fr * dy, fz = fr * dz;
-                fix -= fx; fiy -= fy; fiz -= fz;
-                fjx += fx; fjy += fy; fjz += fz;
-            }
-            pj.x = __shfl_sync(FULL_MASK, pj.x, src);
-            pj.y = __shfl_sync(FULL_MASK, pj.y, src);
-            pj.z = __shfl_sync(FULL_MASK, pj.z, src);
-            pj.w = __shfl_sync(FULL_MASK, pj.w, src);
-            lj.x = __shfl_sync(FULL_MASK, lj.x, src);
-            lj.y = __shfl_sync(FULL_MASK, lj.y, src);
-            fjx = __shfl_sync(FULL_MASK, fjx, src);
-            fjy = __shfl_sync(FULL_MASK, fjy, src);
-            fjz = __shfl_sync(FULL_MASK, fjz, src);
-        }
-        double esum = diff ? e64 : (double)e32 * (diag ? 0.5 : 1.0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
-        float sign = 1.0f;
-        if (kind == ROW_DIFF1) {
-            sign = -1.0f;
-            esum = -esum;
-        }
-        if (lane == 0) a.e_tile[(size_t)row * a.row_cap + slot] = esum;
-        unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
-        fix_add(Fp + i, sign * fix);
-        fix_add(Fp + a.NA + i, sign * fiy);
-        fix_add(Fp + 2 * (size_t)a.NA + i, sign * fiz);
-        if (!diag) {
-            int j = J * kTile + lane;
-            fix_add(Fp + j, sign * fjx);
-            fix_add(Fp + a.NA + j, sign * fjy);
-            fix_add(Fp + 2 * (size_t)a.NA + j, sign * fjz);
-        }
-    }
-}
-
-int tiles_kernel_blocks_per_sm() {
-    int n4 = 0, n2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4>, kTileThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2>, kTileThreads, 0);
-    return n4 < n2 ? n4 : n2;
-}
-
-void launch_tiles(const Args& a, int grid, cudaStream_t s) {
-    if (a.method == 4)
-        k_tiles<4><<<grid, kTileThreads, 0, s>>>(a);
-    else
-        k_tiles<2><<<grid, kTileThreads, 0, s>>>(a);
-}
+// (the tile finder and the pair-tile kernel live in tiles.cu)
 
 // ---------------------------------------------------------------------------
 // exceptions: FP64, user-order positions; one CTA per 256 exceptions of a replica

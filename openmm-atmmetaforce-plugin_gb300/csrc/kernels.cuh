@@ -106,7 +106,8 @@ struct Args {
     const int* dx_start;      // NB+1: cross-class exclusion tiles (difference rows)
     const int2* dx_ent;
     const uint32_t* masks;    // 32 words per mask
-    int4* tiles;              // tile_cap: (I, J, row | kind<<28, (mask+1) | slot<<20)
+    int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
+    int* tile_j;              // 32 j slots per tile (atom tiles)
     double* e_tile;           // nrows*row_cap
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]

@@ -1,0 +1,374 @@
+// Pair-tile lists and the pair-tile kernel (direct-space LJ + reaction field /
+// Ewald) of the ATM evaluation path, sm_103a.
+//
+// A "row" is one 32-atom block I at one geometry (state 1, state 2, or one of the
+// two geometries of the ligand-difference tiles).  k_find builds, per row:
+//   - block tiles: (I, J) for the diagonal tile and every block pair holding an
+//     exclusion, with a 32 x 32 exclusion mask;
+//   - atom tiles: the atoms j of every other candidate block J (bounding boxes
+//     closer than the cutoff) that lie within the cutoff of block I's bounding
+//     box, packed 32 per tile.
+// The per-atom test removes most of the pair slots a 32 x 32 block tile would
+// spend beyond the cutoff.
+//
+// Tile entry (int4):
+//   x = I
+//   y = J (block tiles)
+//   z = row | kind << 28 | atom_tile << 30
+//   w = aux | slot << 20 | pbc << 31
+//       aux  = mask id + 1 (block tiles) or number of valid j (atom tiles)
+//       slot = position of the tile within its row (energy slot)
+//       pbc  = 1 when every pair needs its own minimum image (small boxes)
+#include "kernels.cuh"
+
+namespace atm {
+
+#define FULL_MASK 0xffffffffu
+
+constexpr int kFindWarps = 4;
+
+__device__ __forceinline__ void fix_add_t(unsigned long long* p, float v) {
+    atomicAdd(p, (unsigned long long)__float2ll_rn(v * kFixScaleF));
+}
+
+__device__ __forceinline__ float min_img(float d, float L, float iL) { return d - L * rintf(d * iL); }
+
+__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj, const RepDev& R, float rc2) {
+    float dx = fmaxf(0.f, fabsf(min_img(cj.x - ci.x, R.box[0], R.ibox[0])) - hi.x - hj.x);
+    float dy = fmaxf(0.f, fabsf(min_img(cj.y - ci.y, R.box[1], R.ibox[1])) - hi.y - hj.y);
+    float dz = fmaxf(0.f, fabsf(min_img(cj.z - ci.z, R.box[2], R.ibox[2])) - hi.z - hj.z);
+    return dx * dx + dy * dy + dz * dz < rc2;
+}
+
+__device__ __forceinline__ bool point_close(float4 ci, float4 hi, float4 p, const RepDev& R, float rc2) {
+    float dx = fmaxf(0.f, fabsf(min_img(p.x - ci.x, R.box[0], R.ibox[0])) - hi.x);
+    float dy = fmaxf(0.f, fabsf(min_img(p.y - ci.y, R.box[1], R.ibox[1])) - hi.y);
+    float dz = fmaxf(0.f, fabsf(min_img(p.z - ci.z, R.box[2], R.ibox[2])) - hi.z);
+    return dx * dx + dy * dy + dz * dz < rc2;
+}
+
+// Centre and half extent of block I at the geometry of a row.
+__device__ __forceinline__ void row_box(const Args& a, int I, int kind, float4& c, float4& h) {
+    if (kind == ROW_STATE2) {
+        c = a.bb_c2[I];
+        h = a.bb_h2[I];
+    } else {
+        c = a.bb_c[I];
+        h = a.bb_h[I];
+        if (kind == ROW_DIFF2) {
+            float4 d = a.block_d[I];
+            c.x += d.x;
+            c.y += d.y;
+            c.z += d.z;
+        }
+    }
+}
+
+// One pass over the candidate blocks of a row (bounding boxes closer than the
+// cutoff, no exclusion with I) and their atoms within the cutoff of block I's
+// box.  Counts the atoms; with out != nullptr also writes them, in a fixed
+// order, to consecutive j slots.
+__device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
+                                         const int2* ee, int e0, int e1, int lane, int* out) {
+    const bool diff = kind >= ROW_DIFF1;
+    const bool g2 = kind == ROW_DIFF2;
+    const int cls_i = a.block_cls[I];
+    const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
+    int natom = 0;
+    const int jb = diff ? R.block_begin : I + 1;
+    for (int base = jb; base < R.block_end; base += 32) {
+        const int Jl = base + lane;
+        bool ok = Jl < R.block_end;
+        if (ok && diff) {
+            const int cj = a.block_cls[Jl];
+            ok = Jl != I && cj != cls_i && (cj == 0 || cls_i < cj);
+        }
+        if (ok) {
+            float4 cj4, hj4;
+            if (kind == ROW_STATE2) {
+                cj4 = a.bb_c2[Jl];
+                hj4 = a.bb_h2[Jl];
+            } else {
+                cj4 = a.bb_c[Jl];
+                hj4 = a.bb_h[Jl];
+                if (g2) {
+                    const float4 dd = a.block_d[Jl];  // zero for blocks that do not move
+                    cj4.x += dd.x;
+                    cj4.y += dd.y;
+                    cj4.z += dd.z;
+                }
+            }
+            ok = boxes_close(ci, hi, cj4, hj4, R, a.rc2);
+            for (int k = e0; ok && k < e1; k++)
+                if (ee[k].x == Jl) ok = false;
+        }
+        unsigned cand = __ballot_sync(FULL_MASK, ok);
+        while (cand) {
+            const int J = base + __ffs(cand) - 1;
+            cand &= cand - 1;
+            const int j = J * kTile + lane;
+            bool in = a.orig[j] >= 0;
+            if (in) {
+                float4 p = P[j];
+                if (g2) {
+                    const float4 dd = a.displ[j];
+                    p.x += dd.x;
+                    p.y += dd.y;
+                    p.z += dd.z;
+                }
+                in = point_close(ci, hi, p, R, a.rc2);
+            }
+            const unsigned bal = __ballot_sync(FULL_MASK, in);
+            if (out && in) out[natom + __popc(bal & ((1u << lane) - 1u))] = j;
+            natom += __popc(bal);
+        }
+    }
+    return natom;
+}
+
+__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int row = blockIdx.x * kFindWarps + w;
+    if (row >= a.nrows) return;
+    const int4 d = a.row_desc[row];
+    const int I = d.x, kind = d.y;
+    const RepDev& R = a.reps[d.z];
+    const bool diff = kind >= ROW_DIFF1;
+    const int* es = diff ? a.dx_start : a.ex_start;
+    const int2* ee = diff ? a.dx_ent : a.ex_ent;
+    const int e0 = es[I], e1 = es[I + 1];
+    float4 ci, hi;
+    row_box(a, I, kind, ci, hi);
+    const int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, nullptr);
+    const int nblock = e1 - e0;
+    const int natile = (natom + 31) / 32;
+    int n = nblock + natile;
+    if (lane == 0) atomicMax(&a.status->max_row, n);
+    if (n > a.row_cap) {
+        if (lane == 0) atomicOr(&a.status->overflow, 2);
+        n = 0;  // the evaluation is repeated with larger buffers
+    }
+    int tbase = 0;
+    if (lane == 0) tbase = atomicAdd(&a.status->tile_count, n);
+    tbase = __shfl_sync(FULL_MASK, tbase, 0);
+    if (lane == 0) a.row_count[row] = n;
+    if (n == 0) return;
+    if (tbase + n > a.tile_cap) {
+        if (lane == 0) atomicOr(&a.status->overflow, 1);
+        return;
+    }
+    // second pass: the same atoms, in the same order, straight into the j slots
+    int* out = a.tile_j + (size_t)(tbase + nblock) * 32;
+    row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out);
+    for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
+    // pbc: some pair of an atom tile may need its own minimum image when the
+    // cutoff sphere around block I reaches half a box length
+    const float rc = sqrtf(a.rc2);
+    const unsigned pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
+                          rc + 2.f * hi.z >= 0.5f * R.box[2])
+                             ? 1u
+                             : 0u;
+    const int zword = row | (kind << 28);
+    for (int k = lane; k < nblock; k += 32) {
+        const int2 e = ee[e0 + k];
+        a.tiles[tbase + k] = make_int4(I, e.x, zword, (int)((unsigned)(e.y + 1) | ((unsigned)k << 20) | (1u << 31)));
+    }
+    for (int k = lane; k < natile; k += 32) {
+        const int cnt = min(32, natom - 32 * k);
+        a.tiles[tbase + nblock + k] =
+            make_int4(I, 0, zword | (1 << 30), (int)((unsigned)cnt | ((unsigned)(nblock + k) << 20) | (pbc << 31)));
+    }
+}
+
+void launch_find(const Args& a, cudaStream_t s) {
+    int blocks = (a.nrows + kFindWarps - 1) / kFindWarps;
+    k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
+}
+
+// erfc(x) for x >= 0: Abramowitz & Stegun, Handbook of Mathematical Functions,
+// eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term.
+__device__ __forceinline__ float erfc_as(float x, float expmx2) {
+    const float t = __fdividef(1.0f, 1.0f + 0.3275911f * x);
+    const float p =
+        t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
+    return p * expmx2;
+}
+
+// Energy e and fr = -(dE/dr)/r of one pair (q already scaled by sqrt(k_e),
+// eps4 = 4 sqrt(eps_i eps_j), sig = (sigma_i + sigma_j)/2).
+template <int METHOD>
+__device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float eps4, float alpha, float krf, float crf,
+                                          float& e, float& fr) {
+    const float invr = rsqrtf(r2);
+    const float invr2 = invr * invr;
+    const float s2 = sig * sig * invr2;
+    const float s6 = s2 * s2 * s2;
+    const float t6 = eps4 * s6;
+    e = t6 * s6 - t6;
+    fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
+    if (METHOD == 4) {
+        const float r = r2 * invr;
+        const float ar = alpha * r;
+        const float ex = __expf(-ar * ar);
+        const float ec = erfc_as(ar, ex) * invr;
+        e += qq * ec;
+        fr += qq * (ec + 1.1283791670955126f * alpha * ex) * invr2;
+    } else {
+        e += qq * (invr + krf * r2 - crf);
+        fr += qq * (invr * invr2 - 2.0f * krf);
+    }
+}
+
+// The 32 steps of one tile: lane l meets j-slot (l+k)&31 at step k; j data are
+// read from shared memory, j forces travel with their slot by warp shuffles.
+template <int METHOD, bool PBC, bool DIFF>
+__device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
+                                           float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
+                                           float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
+                                           float crf, float3& fi, float3& fj, float& e32, double& e64) {
+    const int src = (lane + 1) & 31;
+#pragma unroll 8
+    for (int k = 0; k < 32; k++) {
+        const int jl = (lane + k) & 31;
+        const float4 pj = sp[jl];
+        const float2 lj = sl[jl];
+        float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        if (PBC) {
+            dx = min_img(dx, Lx, iLx);
+            dy = min_img(dy, Ly, iLy);
+            dz = min_img(dz, Lz, iLz);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const bool inc = ((mask >> k) & 1u) && r2 < rc2;
+        float e, fr;
+        pair_eval<METHOD>(inc ? r2 : 1.0f, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
+        e = inc ? e : 0.0f;
+        fr = inc ? fr : 0.0f;
+        if (DIFF) e64 += (double)e;
+        else e32 += e;
+        const float fx = fr * dx, fy = fr * dy, fz = fr * dz;
+        fi.x -= fx;
+        fi.y -= fy;
+        fi.z -= fz;
+        fj.x = __shfl_sync(FULL_MASK, fj.x + fx, src);
+        fj.y = __shfl_sync(FULL_MASK, fj.y + fy, src);
+        fj.z = __shfl_sync(FULL_MASK, fj.z + fz, src);
+    }
+}
+
+template <int METHOD>
+__global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
+    __shared__ float4 s_p[kTileThreads / 32][32];
+    __shared__ float2 s_l[kTileThreads / 32][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int ntiles = a.status->tile_count;
+    if (ntiles > a.tile_cap) ntiles = a.tile_cap;
+    const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
+    for (int t = gw; t < ntiles; t += nw) {
+        const int4 T = a.tiles[t];
+        const int I = T.x;
+        const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
+        const int row = z & 0x0fffffffu, kind = (z >> 28) & 3u;
+        const bool atom_tile = (z >> 30) & 1u;
+        const int aux = wd & 0xfffffu, slot = (wd >> 20) & 0x7ffu;
+        const bool pbc = wd >> 31;
+        const RepDev& R = a.reps[a.block_rep[I]];
+        const float Lx = R.box[0], Ly = R.box[1], Lz = R.box[2];
+        const float iLx = R.ibox[0], iLy = R.ibox[1], iLz = R.ibox[2];
+        const bool diff = kind >= ROW_DIFF1, g2 = kind == ROW_DIFF2;
+        const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
+        const int i = I * kTile + lane;
+        float4 pi = P[i];
+        const float2 li = a.lj[i];
+        int j;
+        unsigned mask;
+        bool jvalid = true;
+        if (atom_tile) {
+            j = a.tile_j[(size_t)t * 32 + lane];
+            const unsigned vb = aux >= 32 ? FULL_MASK : ((1u << aux) - 1u);
+            mask = __funnelshift_r(vb, vb, lane);  // bit k: j-slot (lane+k)&31 is a real atom
+            jvalid = lane < aux;
+            if (!jvalid) j = i;
+        } else {
+            j = T.y * kTile + lane;
+            mask = a.masks[(size_t)(aux - 1) * 32 + lane];
+        }
+        float4 pj = P[j];
+        const float2 lj = a.lj[j];
+        if (g2) {
+            const float4 di = a.displ[i], dj = a.displ[j];
+            pi.x += di.x;
+            pi.y += di.y;
+            pi.z += di.z;
+            pj.x += dj.x;
+            pj.y += dj.y;
+            pj.z += dj.z;
+        }
+        if (!pbc) {
+            // the image of j nearest block I's centre is the minimum image for every i of the block
+            float4 c, h;
+            row_box(a, I, kind, c, h);
+            pj.x = c.x + min_img(pj.x - c.x, Lx, iLx);
+            pj.y = c.y + min_img(pj.y - c.y, Ly, iLy);
+            pj.z = c.z + min_img(pj.z - c.z, Lz, iLz);
+            pi.x = c.x + min_img(pi.x - c.x, Lx, iLx);
+            pi.y = c.y + min_img(pi.y - c.y, Ly, iLy);
+            pi.z = c.z + min_img(pi.z - c.z, Lz, iLz);
+        }
+        s_p[w][lane] = pj;
+        s_l[w][lane] = lj;
+        __syncwarp();
+        float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
+        float e32 = 0.f;
+        double e64 = 0.0;
+        if (diff) {
+            if (pbc)
+                tile_steps<METHOD, true, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                               alpha, krf, crf, fi, fj, e32, e64);
+            else
+                tile_steps<METHOD, false, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                alpha, krf, crf, fi, fj, e32, e64);
+        } else {
+            if (pbc)
+                tile_steps<METHOD, true, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                alpha, krf, crf, fi, fj, e32, e64);
+            else
+                tile_steps<METHOD, false, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                 alpha, krf, crf, fi, fj, e32, e64);
+        }
+        __syncwarp();
+        const bool diag = !atom_tile && T.y == I;
+        double esum = diff ? e64 : (double)e32 * (diag ? 0.5 : 1.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+        const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
+        if (lane == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
+        unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
+        fix_add_t(Fp + i, sign * fi.x);
+        fix_add_t(Fp + a.NA + i, sign * fi.y);
+        fix_add_t(Fp + 2 * (size_t)a.NA + i, sign * fi.z);
+        if (!diag && jvalid) {
+            fix_add_t(Fp + j, sign * fj.x);
+            fix_add_t(Fp + a.NA + j, sign * fj.y);
+            fix_add_t(Fp + 2 * (size_t)a.NA + j, sign * fj.z);
+        }
+    }
+}
+
+int tiles_kernel_blocks_per_sm() {
+    int n4 = 0, n2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2>, kTileThreads, 0);
+    return n4 < n2 ? n4 : n2;
+}
+
+void launch_tiles(const Args& a, int grid, cudaStream_t s) {
+    if (a.method == 4)
+        k_tiles<4><<<grid, kTileThreads, 0, s>>>(a);
+    else
+        k_tiles<2><<<grid, kTileThreads, 0, s>>>(a);
+}
+
+}  // namespace atm
