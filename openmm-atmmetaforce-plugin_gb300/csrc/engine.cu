@@ -555,7 +555,6 @@ void Engine::build_layout() {
             long long G3 = (long long)rd.K[0] * rd.K[1] * rd.K[2];
             long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
             rd.real_off = n_real_;
-            rd.fixed_off = n_real_;
             rd.cplx_off = n_cplx_;
             n_real_ += 2 * G3;
             n_cplx_ += 2 * C3;
@@ -565,6 +564,20 @@ void Engine::build_layout() {
                 rd.mod_off[a] = (int)moduli_.size();
                 for (double v : m) moduli_.push_back((float)v);
             }
+        }
+        // spreading bricks: at most 16 grid points per dimension, two grids per replica
+        brick_cta_rep_.clear();
+        brick_smem_ = 0;
+        for (int r = 0; r < R_; r++) {
+            RepDev& rd = rep_host_[r];
+            for (int d = 0; d < 3; d++) {
+                rd.nbrick[d] = (rd.K[d] + 15) / 16;
+                rd.bsz[d] = (rd.K[d] + rd.nbrick[d] - 1) / rd.nbrick[d];
+            }
+            rd.brick_cta_b = (int)brick_cta_rep_.size();
+            int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
+            for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
+            brick_smem_ = std::max(brick_smem_, (int)(sizeof(unsigned long long) * rd.bsz[0] * rd.bsz[1] * rd.bsz[2]));
         }
         for (int r = 0; r < R_; r++) {
             RepDev& rd = rep_host_[r];
@@ -657,6 +670,13 @@ void Engine::alloc_device() {
     a.block_rep = dupload(d_allocs_, block_rep_);
     a.block_cls = dupload(d_allocs_, block_cls_);
     a.block_d = dupload(d_allocs_, block_d_);
+    {
+        std::vector<int> mov;
+        for (int b = 0; b < NB_; b++)
+            if (block_cls_[b] != 0) mov.push_back(b);
+        a.n_mov_blocks = (int)mov.size();
+        a.mov_blocks = dupload(d_allocs_, mov);
+    }
     a.bb_c = dalloc<float4>(d_allocs_, NB_);
     a.bb_h = dalloc<float4>(d_allocs_, NB_);
     a.bb_c2 = full_ ? dalloc<float4>(d_allocs_, NB_) : nullptr;
@@ -681,8 +701,9 @@ void Engine::alloc_device() {
     a.e_part_exc = dalloc<double>(d_allocs_, 3 * (size_t)std::max(1, a.exc_ctas));
     a.n_real_total = n_real_;
     if (method_ == NonbondedForce::PME) {
-        a.qfix = dalloc<unsigned long long>(d_allocs_, n_real_);
-        CUDA_CHECK(cudaMemset(a.qfix, 0, sizeof(unsigned long long) * n_real_));
+        a.brick_ctas = (int)brick_cta_rep_.size();
+        a.brick_smem = brick_smem_;
+        a.brick_cta_rep = dupload(d_allocs_, brick_cta_rep_);
         a.qreal = dalloc<float>(d_allocs_, n_real_);
         a.qcplx = dalloc<float2>(d_allocs_, n_cplx_);
         a.moduli = dupload(d_allocs_, moduli_);
@@ -741,7 +762,12 @@ void Engine::update_rep_table() {
 int Engine::launches_per_eval() const {
     // prepare, find, tiles, exceptions, finalize, output, matrix (+ PME kernels)
     int n = 4 + 3;
-    if (method_ == NonbondedForce::PME) n += 4;
+    if (method_ == NonbondedForce::PME) n += 3;  // spread, conv, gather
+    if (method_ == NonbondedForce::PME && !full_) {
+        bool any = false;
+        for (int c : block_cls_) any |= c != 0;
+        n += any ? 1 : 0;  // gather of the moving atoms
+    }
     return n;
 }
 
@@ -759,7 +785,6 @@ void Engine::record(cudaStream_t st, bool host_io) {
         CUDA_CHECK(cudaEventRecord(ev_fork_, st));
         CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork_, 0));
         launch_spread(a, s_pme_);
-        launch_convert(a, s_pme_);
         for (auto& g : groups_)
             CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
         launch_conv(a, s_pme_);
@@ -847,8 +872,6 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos) {
                 }
                 launch_spread(a, st);
                 mark("spread");
-                launch_convert(a, st);
-                mark("convert");
                 for (auto& g : groups_)
                     CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
                 mark("fft_r2c");

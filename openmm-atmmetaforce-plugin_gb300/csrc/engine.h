@@ -118,6 +118,8 @@ private:
     std::vector<int> exc_cta_first_;
     std::vector<int> conv_cta_rep_;
     std::vector<long long> conv_cta_first_;
+    std::vector<int> brick_cta_rep_;
+    int brick_smem_ = 0;
     std::vector<float> moduli_;
     std::vector<RepDev> rep_host_;
     long long n_real_ = 0, n_cplx_ = 0;

@@ -40,8 +40,10 @@ __device__ __forceinline__ float wrapf(float x, float L, float iL) { return x - 
 // ---------------------------------------------------------------------------
 // prepare: one warp per block
 // ---------------------------------------------------------------------------
+// Bounding box of a block (minimum image relative to its first atom); h.w
+// receives the number of real (non-padding) atoms of the block.
 __device__ __forceinline__ void warp_bbox(float x, float y, float z, const RepDev& R, float4* c, float4* h,
-                                          int lane) {
+                                          int lane, int nreal) {
     float x0 = __shfl_sync(FULL_MASK, x, 0), y0 = __shfl_sync(FULL_MASK, y, 0), z0 = __shfl_sync(FULL_MASK, z, 0);
     float dx = x - x0, dy = y - y0, dz = z - z0;
     dx -= R.box[0] * rintf(dx * R.ibox[0]);
@@ -59,7 +61,7 @@ __device__ __forceinline__ void warp_bbox(float x, float y, float z, const RepDe
     }
     if (lane == 0) {
         *c = make_float4(x0 + 0.5f * (lx + hx), y0 + 0.5f * (ly + hy), z0 + 0.5f * (lz + hz), 0.f);
-        *h = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), 0.f);
+        *h = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), __int_as_float(nreal));
     }
 }
 
@@ -71,6 +73,7 @@ __global__ void k_prepare(Args a) {
     int rep = a.block_rep[b];
     const RepDev& R = a.reps[rep];
     int o = a.orig[s];
+    const int nreal = __popc(__ballot_sync(FULL_MASK, o >= 0));  // padding sits at the end of a block
     if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
     const double* p = a.pos_in + 3 * (size_t)(R.in_off + o);
     float x = (float)(p[0] - R.boxd[0] * floor(p[0] / R.boxd[0]));
@@ -79,14 +82,14 @@ __global__ void k_prepare(Args a) {
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
     for (int k = 0; k < 6; k++) a.F[(size_t)k * a.NA + s] = 0ull;
-    warp_bbox(x, y, z, R, &a.bb_c[b], &a.bb_h[b], lane);
+    warp_bbox(x, y, z, R, &a.bb_c[b], &a.bb_h[b], lane, nreal);
     if (a.full) {
         float4 d = a.displ[s];
         float x2 = wrapf(x + d.x, R.box[0], R.ibox[0]);
         float y2 = wrapf(y + d.y, R.box[1], R.ibox[1]);
         float z2 = wrapf(z + d.z, R.box[2], R.ibox[2]);
         a.posq2[s] = make_float4(x2, y2, z2, q);
-        warp_bbox(x2, y2, z2, R, &a.bb_c2[b], &a.bb_h2[b], lane);
+        warp_bbox(x2, y2, z2, R, &a.bb_c2[b], &a.bb_h2[b], lane, nreal);
     }
     if (b == 0 && lane == 0) {
         a.status->tile_count = 0;
@@ -250,76 +253,208 @@ __device__ __forceinline__ void make_stencil(float x, float y, float z, const Re
     }
 }
 
-__device__ __forceinline__ void spread_one(unsigned long long* G, const RepDev& R, const Stencil& S, float q) {
-    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
-    int iz[5];
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        int v = S.base[2] - c;
-        iz[c] = v < 0 ? v + Kz : v;
-    }
-#pragma unroll
-    for (int a0 = 0; a0 < 5; a0++) {
-        int ix = S.base[0] - a0;
-        if (ix < 0) ix += Kx;
-        float wa = q * S.w[0][a0];
-#pragma unroll
-        for (int b0 = 0; b0 < 5; b0++) {
-            int iy = S.base[1] - b0;
-            if (iy < 0) iy += Ky;
-            float wab = wa * S.w[1][b0];
-            size_t rowb = ((size_t)ix * Ky + iy) * Kz;
-#pragma unroll
-            for (int c0 = 0; c0 < 5; c0++) fix_add(G + rowb + iz[c0], wab * S.w[2][c0]);
-        }
-    }
+// Charge spreading by bricks.  One CTA owns one brick (at most 16^3 points) of
+// one of a replica's two charge grids.  It finds the 32-atom blocks whose
+// stencils can reach the brick (bounding boxes in grid units, one point of
+// margin for rounding), accumulates their contributions as int64 fixed point
+// in shared memory (exact and order independent), and writes every point of
+// its brick once as a float.  Grid 0: state 1.  Grid 1: state 2 (two-state mode)
+// or the structure-factor update of the moving atoms, -q at x and +q at x + d
+// (difference mode).
+constexpr int kBrickThreads = 256;
+
+// Does the cyclic range of base indices of a box (centre c, half extent h, nm)
+// meet the cyclic interval [o, o + len) of Z_K?
+__device__ __forceinline__ bool cyc_meet(float c, float h, float iL, int K, int o, int len) {
+    const int lo = (int)floorf((c - h) * iL * (float)K) - 1;
+    const int n = (int)floorf((c + h) * iL * (float)K) + 1 - lo + 1;
+    if (n >= K) return true;
+    int A = lo % K;
+    if (A < 0) A += K;
+    int d1 = o - A;
+    if (d1 < 0) d1 += K;
+    int d2 = A - o;
+    if (d2 < 0) d2 += K;
+    return d1 < n || d2 < len;
 }
 
-__global__ void k_spread(Args a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.NA) return;
-    int b = s >> 5;
-    const RepDev& R = a.reps[a.block_rep[b]];
-    float4 p = a.posq[s];
-    if (p.w == 0.0f) return;
-    size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
-    unsigned long long* G1 = a.qfix + R.fixed_off;
-    unsigned long long* G2 = G1 + G3;
-    Stencil S;
-    make_stencil(p.x, p.y, p.z, R, S, false);
-    spread_one(G1, R, S, p.w);
-    if (a.full) {
-        float4 p2 = a.posq2[s];
-        make_stencil(p2.x, p2.y, p2.z, R, S, false);
-        spread_one(G2, R, S, p.w);
-    } else if (a.block_cls[b] != 0) {
-        // structure-factor update of the moving atoms: -q at x, +q at x + d
-        spread_one(G2, R, S, -p.w);
-        float4 d = a.displ[s];
-        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
-                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, false);
-        spread_one(G2, R, S, p.w);
+__device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev& R, const int* o, const int* e) {
+    return cyc_meet(c.x, h.x, R.ibox[0], R.K[0], o[0], e[0] + kOrder - 1) &&
+           cyc_meet(c.y, h.y, R.ibox[1], R.K[1], o[1], e[1] + kOrder - 1) &&
+           cyc_meet(c.z, h.z, R.ibox[2], R.K[2], o[2], e[2] + kOrder - 1);
+}
+
+constexpr int kSpreadChunk = kBrickThreads;  // blocks examined per pass (one per thread)
+constexpr int kSpreadBatch = 16;             // candidate blocks whose atoms are listed at once
+constexpr int kSpreadList = kSpreadBatch * kTile;
+constexpr int kStencilFloats = 3 * kOrder;   // q*wx, wy, wz of one listed atom
+
+// Dynamic shared memory of a spreading CTA: accumulators plus listed stencils.
+int spread_smem_bytes(int accum_bytes) { return accum_bytes + kSpreadList * kStencilFloats * (int)sizeof(float); }
+
+__device__ __forceinline__ float pick5(const float* w, int k) {
+    return k == 0 ? w[0] : k == 1 ? w[1] : k == 2 ? w[2] : k == 3 ? w[3] : w[4];
+}
+
+// Position and signed charge of a spreading entry (code: 0 state 1 +q, 1 state 1
+// -q, 2 state 2 +q, 3 state 1 displaced +q).
+__device__ __forceinline__ float4 entry_atom(const Args& a, const RepDev& R, int s, int code) {
+    float4 p = code == 2 ? a.posq2[s] : a.posq[s];
+    if (code == 1) p.w = -p.w;
+    if (code == 3) {
+        const float4 dd = a.displ[s];
+        p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
+        p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
+        p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
+    }
+    return p;
+}
+
+// Local index of grid point base - k in a brick [o, o + e), or -1.
+__device__ __forceinline__ int brick_local(int base, int k, int o, int e, int K) {
+    int v = base - k - o;
+    v += v < 0 ? K : 0;
+    v += v < 0 ? K : 0;
+    return v < e ? v : -1;
+}
+
+__global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
+    // int64 fixed-point sums kept exactly as two 32-bit words: hi (value >> 16,
+    // signed) and lo (value & 0xffff), so that native 32-bit shared atomics suffice
+    extern __shared__ int s_acc[];
+    __shared__ int s_cand[2 * kSpreadChunk];
+    __shared__ int s_list[kSpreadList];
+    __shared__ int s_ncand, s_nlist;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c = blockIdx.x;
+    const RepDev& R = a.reps[a.brick_cta_rep[c]];
+    const int nb = R.nbrick[0] * R.nbrick[1] * R.nbrick[2];
+    const int local = c - R.brick_cta_b;
+    const int g = local / nb, b = local % nb;
+    const int bi[3] = {b / (R.nbrick[1] * R.nbrick[2]), (b / R.nbrick[2]) % R.nbrick[1], b % R.nbrick[2]};
+    int o[3], e[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        o[d] = bi[d] * R.bsz[d];
+        e[d] = min(R.bsz[d], R.K[d] - o[d]);
+    }
+    const int npts = e[0] * e[1] * e[2];
+    const int cap_pts = a.brick_smem / 8;
+    int* s_hi = s_acc;
+    unsigned* s_lo = (unsigned*)(s_acc + cap_pts);
+    float* s_w = (float*)(s_acc + 2 * cap_pts);
+    for (int k = tid; k < npts; k += kBrickThreads) {
+        s_hi[k] = 0;
+        s_lo[k] = 0u;
+    }
+    for (int base = R.block_begin; base < R.block_end; base += kSpreadChunk) {
+        if (tid == 0) s_ncand = 0;
+        __syncthreads();
+        // 1. blocks whose bounding box reaches the brick
+        const int J = base + tid;
+        if (J < R.block_end) {
+            if (g == 0) {
+                if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = J << 2;
+            } else if (a.full) {
+                if (box_meets_brick(a.bb_c2[J], a.bb_h2[J], R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 2;
+            } else if (a.block_cls[J] != 0) {
+                const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
+                const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
+                if (box_meets_brick(c1, h1, R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 1;
+                if (box_meets_brick(c2, h1, R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 3;
+            }
+        }
+        __syncthreads();
+        const int nc = s_ncand;
+        for (int cb = 0; cb < nc; cb += kSpreadBatch) {
+            if (tid == 0) s_nlist = 0;
+            __syncthreads();
+            // 2. atoms of those blocks whose stencil reaches the brick (lanes = atoms)
+            const int ce = min(nc, cb + kSpreadBatch);
+            for (int ci = cb + warp; ci < ce; ci += kBrickThreads / 32) {
+                const int ent = s_cand[ci];
+                const int Jc = ent >> 2, code = ent & 3;
+                const int s = Jc * kTile + lane;
+                bool ok = lane < __float_as_int(a.bb_h[Jc].w);
+                if (ok) {
+                    const float4 p = entry_atom(a, R, s, code);
+                    ok = p.w != 0.0f;
+                    const float cc[3] = {p.x, p.y, p.z};
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        float f = cc[d] * R.ibox[d];
+                        f -= floorf(f);
+                        int bs = (int)floorf(f * (float)R.K[d]);
+                        if (bs >= R.K[d]) bs -= R.K[d];
+                        int v = bs - o[d];
+                        v += v < 0 ? R.K[d] : 0;
+                        ok = ok && v < e[d] + kOrder - 1;
+                    }
+                }
+                const unsigned bal = __ballot_sync(FULL_MASK, ok);
+                int pos = 0;
+                if (lane == 0 && bal) pos = atomicAdd(&s_nlist, __popc(bal));
+                pos = __shfl_sync(FULL_MASK, pos, 0);
+                if (ok) {
+                    // each listed atom's stencil, computed once: q*wx, wy, wz and
+                    // the brick-local indices of its first stencil point
+                    const int li = pos + __popc(bal & ((1u << lane) - 1u));
+                    const float4 p = entry_atom(a, R, s, code);
+                    Stencil S;
+                    make_stencil(p.x, p.y, p.z, R, S, false);
+                    float* wv = s_w + li * kStencilFloats;
+#pragma unroll
+                    for (int k = 0; k < kOrder; k++) {
+                        wv[k] = p.w * S.w[0][k];
+                        wv[kOrder + k] = S.w[1][k];
+                        wv[2 * kOrder + k] = S.w[2][k];
+                    }
+                    s_list[li] = (S.base[0] << 20) | (S.base[1] << 10) | S.base[2];
+                }
+            }
+            __syncthreads();
+            // 3. one atom per warp, lanes over the 5 x 5 (y, z) stencil offsets
+            const int nl = s_nlist;
+            const int b0 = lane / kOrder, c0 = lane % kOrder;
+            for (int li = warp; li < nl; li += kBrickThreads / 32) {
+                if (lane >= kOrder * kOrder) continue;
+                const int bases = s_list[li];
+                const float* wv = s_w + li * kStencilFloats;
+                const int ly = brick_local((bases >> 10) & 1023, b0, o[1], e[1], R.K[1]);
+                const int lz = brick_local(bases & 1023, c0, o[2], e[2], R.K[2]);
+                if (ly < 0 || lz < 0) continue;
+                const float wy = wv[kOrder + b0], wz = wv[2 * kOrder + c0];
+                const int bx = bases >> 20;
+#pragma unroll
+                for (int a0 = 0; a0 < kOrder; a0++) {
+                    const int lx = brick_local(bx, a0, o[0], e[0], R.K[0]);
+                    if (lx < 0) continue;
+                    const float v = wv[a0] * wy * wz;
+                    const long long q64 = __float2ll_rn(v * kFixScaleF);
+                    const int idx = (lx * e[1] + ly) * e[2] + lz;
+                    atomicAdd(&s_hi[idx], (int)(q64 >> 16));
+                    atomicAdd(&s_lo[idx], (unsigned)(q64 & 0xffff));
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    float* G = a.qreal + R.real_off + (size_t)g * G3;
+    for (int k = tid; k < npts; k += kBrickThreads) {
+        const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
+        const long long v = (long long)s_hi[k] * 65536ll + (long long)s_lo[k];
+        G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = (float)((double)v * (1.0 / kFixScale));
     }
 }
 
 void launch_spread(const Args& a, cudaStream_t s) {
-    k_spread<<<(a.NA + 127) / 128, 128, 0, s>>>(a);
-}
-
-// fixed-point charge grids -> float grids; clears the fixed-point grids
-__global__ void k_convert(Args a) {
-    size_t n = (size_t)a.n_real_total;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-        long long v = (long long)a.qfix[k];
-        a.qfix[k] = 0ull;
-        a.qreal[k] = (float)((double)v * (1.0 / kFixScale));
-    }
-}
-
-void launch_convert(const Args& a, cudaStream_t s) {
-    int blocks = (int)((a.n_real_total + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_convert<<<blocks, 256, 0, s>>>(a);
+    if (a.brick_ctas <= 0) return;
+    const int bytes = spread_smem_bytes(a.brick_smem);
+    // opt in to more than 48 KB of dynamic shared memory (per device; this runs
+    // when the evaluation graph is recorded, not at every evaluation)
+    cudaFuncSetAttribute(k_spread, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    k_spread<<<a.brick_ctas, kBrickThreads, bytes, s>>>(a);
 }
 
 // reciprocal-space convolution on the half spectrum; energies per CTA
@@ -415,56 +550,117 @@ __device__ __forceinline__ void gather_one(const float* G, const RepDev& R, cons
     }
 }
 
-__global__ void k_gather(Args a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+// Gradients of two grids at one stencil (the state-1 potential and the
+// potential of the moved charges).
+__device__ __forceinline__ void gather_two(const float* G1, const float* G2, const RepDev& R, const Stencil& S,
+                                           float* g1, float* g2) {
+    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
+    int iz[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        int v = S.base[2] - c;
+        iz[c] = v < 0 ? v + Kz : v;
+    }
+    g1[0] = g1[1] = g1[2] = g2[0] = g2[1] = g2[2] = 0.f;
+#pragma unroll
+    for (int a0 = 0; a0 < 5; a0++) {
+        int ix = S.base[0] - a0;
+        if (ix < 0) ix += Kx;
+#pragma unroll
+        for (int b0 = 0; b0 < 5; b0++) {
+            int iy = S.base[1] - b0;
+            if (iy < 0) iy += Ky;
+            const size_t rowo = ((size_t)ix * Ky + iy) * Kz;
+            float s1 = 0.f, z1 = 0.f, s2 = 0.f, z2 = 0.f;
+#pragma unroll
+            for (int c0 = 0; c0 < 5; c0++) {
+                const float v1 = __ldg(G1 + rowo + iz[c0]);
+                const float v2 = __ldg(G2 + rowo + iz[c0]);
+                s1 += S.w[2][c0] * v1;
+                z1 += S.dw[2][c0] * v1;
+                s2 += S.w[2][c0] * v2;
+                z2 += S.dw[2][c0] * v2;
+            }
+            const float dxy = S.dw[0][a0] * S.w[1][b0], xdy = S.w[0][a0] * S.dw[1][b0], xy = S.w[0][a0] * S.w[1][b0];
+            g1[0] += dxy * s1;
+            g1[1] += xdy * s1;
+            g1[2] += xy * z1;
+            g2[0] += dxy * s2;
+            g2[1] += xdy * s2;
+            g2[2] += xy * z2;
+        }
+    }
+}
+
+__device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, int s, float q, float gx, float gy,
+                                               float gz, const RepDev& R) {
+    fix_add(F + s, -q * gx * (float)R.K[0] * R.ibox[0]);
+    fix_add(F + NA + s, -q * gy * (float)R.K[1] * R.ibox[1]);
+    fix_add(F + 2 * (size_t)NA + s, -q * gz * (float)R.K[2] * R.ibox[2]);
+}
+
+// Reciprocal-space forces of every atom that does not move (difference mode)
+// or of every atom at both states (two-state mode).
+__global__ void __launch_bounds__(128, 6) k_gather(Args a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.NA) return;
-    int b = s >> 5;
+    const int b = s >> 5;
+    if (!a.full && a.block_cls[b] != 0) return;  // moving atoms: k_gather_moving
     const RepDev& R = a.reps[a.block_rep[b]];
-    float4 p = a.posq[s];
+    const float4 p = a.posq[s];
     if (p.w == 0.0f) return;
-    size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
     const float* phi1 = a.qreal + R.real_off;
     const float* phi2 = phi1 + G3;
-    const float sx = (float)R.K[0] * R.ibox[0], sy = (float)R.K[1] * R.ibox[1], sz = (float)R.K[2] * R.ibox[2];
+    unsigned long long* F2 = a.F + 3 * (size_t)a.NA;
     Stencil S;
     make_stencil(p.x, p.y, p.z, R, S, true);
-    float gx, gy, gz;
-    gather_one(phi1, R, S, gx, gy, gz);
-    float q = p.w;
-    fix_add(a.F + s, -q * gx * sx);
-    fix_add(a.F + a.NA + s, -q * gy * sy);
-    fix_add(a.F + 2 * (size_t)a.NA + s, -q * gz * sz);
-    unsigned long long* F2 = a.F + 3 * (size_t)a.NA;
     if (a.full) {
-        float4 p2 = a.posq2[s];
+        float gx, gy, gz;
+        gather_one(phi1, R, S, gx, gy, gz);
+        add_grad_force(a.F, a.NA, s, p.w, gx, gy, gz, R);
+        const float4 p2 = a.posq2[s];
         make_stencil(p2.x, p2.y, p2.z, R, S, true);
         gather_one(phi2, R, S, gx, gy, gz);
-        fix_add(F2 + s, -q * gx * sx);
-        fix_add(F2 + a.NA + s, -q * gy * sy);
-        fix_add(F2 + 2 * (size_t)a.NA + s, -q * gz * sz);
-    } else if (a.block_cls[b] == 0) {
-        // F2 - F1 of an atom that does not move: the potential of the moved charges
-        gather_one(phi2, R, S, gx, gy, gz);
-        fix_add(F2 + s, -q * gx * sx);
-        fix_add(F2 + a.NA + s, -q * gy * sy);
-        fix_add(F2 + 2 * (size_t)a.NA + s, -q * gz * sz);
+        add_grad_force(F2, a.NA, s, p.w, gx, gy, gz, R);
     } else {
-        // moving atom: F2 at x+d in phi1+dphi, minus F1 at x in phi1
-        float hx, hy, hz;
-        float4 d = a.displ[s];
-        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
-                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
-        gather_one(phi1, R, S, hx, hy, hz);
-        float kx, ky, kz;
-        gather_one(phi2, R, S, kx, ky, kz);
-        fix_add(F2 + s, -q * (hx + kx - gx) * sx);
-        fix_add(F2 + a.NA + s, -q * (hy + ky - gy) * sy);
-        fix_add(F2 + 2 * (size_t)a.NA + s, -q * (hz + kz - gz) * sz);
+        // F1 from the state-1 potential; F2 - F1 from the potential of the moved charges
+        float g1[3], g2[3];
+        gather_two(phi1, phi2, R, S, g1, g2);
+        add_grad_force(a.F, a.NA, s, p.w, g1[0], g1[1], g1[2], R);
+        add_grad_force(F2, a.NA, s, p.w, g2[0], g2[1], g2[2], R);
     }
+}
+
+// Moving atoms of the difference mode: F1 at x in phi1, and F2 - F1 =
+// F(x + d in phi1 + dphi) - F(x in phi1).
+__global__ void k_gather_moving(Args a) {
+    const int blk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (blk >= a.n_mov_blocks) return;
+    const int b = a.mov_blocks[blk];
+    const int s = b * kTile + (threadIdx.x & 31);
+    const RepDev& R = a.reps[a.block_rep[b]];
+    const float4 p = a.posq[s];
+    if (p.w == 0.0f) return;
+    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    const float* phi1 = a.qreal + R.real_off;
+    const float* phi2 = phi1 + G3;
+    Stencil S;
+    make_stencil(p.x, p.y, p.z, R, S, true);
+    float gx, gy, gz, hx, hy, hz, kx, ky, kz;
+    gather_one(phi1, R, S, gx, gy, gz);
+    add_grad_force(a.F, a.NA, s, p.w, gx, gy, gz, R);
+    const float4 d = a.displ[s];
+    make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
+                 wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
+    gather_one(phi1, R, S, hx, hy, hz);
+    gather_one(phi2, R, S, kx, ky, kz);
+    add_grad_force(a.F + 3 * (size_t)a.NA, a.NA, s, p.w, hx + kx - gx, hy + ky - gy, hz + kz - gz, R);
 }
 
 void launch_gather(const Args& a, cudaStream_t s) {
     k_gather<<<(a.NA + 127) / 128, 128, 0, s>>>(a);
+    if (!a.full && a.n_mov_blocks > 0) k_gather_moving<<<(a.n_mov_blocks + 3) / 4, 128, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------

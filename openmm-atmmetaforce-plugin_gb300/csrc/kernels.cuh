@@ -41,7 +41,9 @@ struct RepDev {
     int mod_off[3];           // offsets of the B-spline moduli (per dimension)
     long long real_off;       // first float of this replica's two real grids
     long long cplx_off;       // first complex of its two spectra
-    long long fixed_off;      // first int64 of its two fixed-point charge grids
+    int nbrick[3];            // spreading bricks per dimension
+    int bsz[3];               // brick size (grid points) per dimension
+    int brick_cta_b;          // first spreading CTA of this replica (2 x bricks CTAs)
     int row1_b, row1_e;       // rows of state 1 (full and difference modes)
     int row2_b, row2_e;       // rows of state 2 (full) or of the difference tiles (diff)
     int exc_cta_b, exc_cta_e; // exception-kernel CTAs (energy partials)
@@ -94,6 +96,8 @@ struct Args {
     const int* block_rep;     // NB
     const int* block_cls;     // NB: displacement class (0 = not moving)
     const float4* block_d;    // NB: displacement of the block's class
+    int n_mov_blocks;         // blocks of moving atoms (all replicas)
+    const int* mov_blocks;
     float4* bb_c;             // NB: bounding-box centres (state 1)
     float4* bb_h;             // NB: half extents
     float4* bb_c2;            // NB: state 2 (full mode)
@@ -120,7 +124,9 @@ struct Args {
     int exc_ctas;
     const int* exc_cta_first; // first exception of each CTA
     // PME
-    unsigned long long* qfix; // fixed-point charge grids
+    int brick_ctas;           // spreading CTAs (all replicas)
+    int brick_smem;           // dynamic shared memory of a spreading CTA (bytes)
+    const int* brick_cta_rep; // replica of each spreading CTA
     float* qreal;             // real grids (charge, then potential)
     float2* qcplx;            // spectra
     const float* moduli;      // B-spline moduli, per replica per dimension
@@ -140,7 +146,6 @@ void launch_find(const Args& a, cudaStream_t s);
 void launch_tiles(const Args& a, int grid, cudaStream_t s);
 void launch_exceptions(const Args& a, cudaStream_t s);
 void launch_spread(const Args& a, cudaStream_t s);
-void launch_convert(const Args& a, cudaStream_t s);
 void launch_conv(const Args& a, cudaStream_t s);
 void launch_gather(const Args& a, cudaStream_t s);
 void launch_finalize(const Args& a, cudaStream_t s);

@@ -66,10 +66,10 @@ __device__ __forceinline__ void row_box(const Args& a, int I, int kind, float4& 
 
 // One pass over the candidate blocks of a row (bounding boxes closer than the
 // cutoff, no exclusion with I) and their atoms within the cutoff of block I's
-// box.  Counts the atoms; with out != nullptr also writes them, in a fixed
-// order, to consecutive j slots.
+// box.  Counts the atoms; with out != nullptr also writes the first cap of them,
+// in a fixed order, to consecutive j slots.
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
-                                         const int2* ee, int e0, int e1, int lane, int* out) {
+                                         const int2* ee, int e0, int e1, int lane, int* out, int cap) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
@@ -103,30 +103,46 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
                 if (ee[k].x == Jl) ok = false;
         }
         unsigned cand = __ballot_sync(FULL_MASK, ok);
+        // two candidate blocks per step so that their loads overlap
         while (cand) {
-            const int J = base + __ffs(cand) - 1;
+            const int J1 = base + __ffs(cand) - 1;
             cand &= cand - 1;
-            const int j = J * kTile + lane;
-            bool in = a.orig[j] >= 0;
-            if (in) {
-                float4 p = P[j];
-                if (g2) {
-                    const float4 dd = a.displ[j];
-                    p.x += dd.x;
-                    p.y += dd.y;
-                    p.z += dd.z;
-                }
-                in = point_close(ci, hi, p, R, a.rc2);
+            const int J2 = cand ? base + __ffs(cand) - 1 : -1;
+            if (cand) cand &= cand - 1;
+            const int j1 = J1 * kTile + lane;
+            const int j2 = (J2 >= 0 ? J2 : J1) * kTile + lane;
+            float4 p1 = P[j1], p2 = P[j2];
+            const int n1 = __float_as_int((kind == ROW_STATE2 ? a.bb_h2 : a.bb_h)[J1].w);
+            const int n2 = J2 >= 0 ? __float_as_int((kind == ROW_STATE2 ? a.bb_h2 : a.bb_h)[J2].w) : 0;
+            if (g2) {
+                const float4 d1 = a.displ[j1], d2 = a.displ[j2];
+                p1.x += d1.x;
+                p1.y += d1.y;
+                p1.z += d1.z;
+                p2.x += d2.x;
+                p2.y += d2.y;
+                p2.z += d2.z;
             }
-            const unsigned bal = __ballot_sync(FULL_MASK, in);
-            if (out && in) out[natom + __popc(bal & ((1u << lane) - 1u))] = j;
-            natom += __popc(bal);
+            const bool in1 = lane < n1 && point_close(ci, hi, p1, R, a.rc2);
+            const bool in2 = lane < n2 && point_close(ci, hi, p2, R, a.rc2);
+            const unsigned b1 = __ballot_sync(FULL_MASK, in1);
+            const unsigned b2 = __ballot_sync(FULL_MASK, in2);
+            if (out) {
+                const unsigned lt = (1u << lane) - 1u;
+                const int k1 = natom + __popc(b1 & lt), k2 = natom + __popc(b1) + __popc(b2 & lt);
+                if (in1 && k1 < cap) out[k1] = j1;
+                if (in2 && k2 < cap) out[k2] = j2;
+            }
+            natom += __popc(b1) + __popc(b2);
         }
     }
     return natom;
 }
 
+constexpr int kStageAtoms = 1024;  // culled atoms staged in shared memory per row
+
 __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
+    __shared__ int s_stage[kFindWarps][kStageAtoms];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int row = blockIdx.x * kFindWarps + w;
     if (row >= a.nrows) return;
@@ -139,7 +155,9 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     const int e0 = es[I], e1 = es[I + 1];
     float4 ci, hi;
     row_box(a, I, kind, ci, hi);
-    const int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, nullptr);
+    // staged in shared memory; rows longer than the stage are written by a second pass
+    const int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, s_stage[w], kStageAtoms);
+    __syncwarp();
     const int nblock = e1 - e0;
     const int natile = (natom + 31) / 32;
     int n = nblock + natile;
@@ -157,9 +175,13 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
         if (lane == 0) atomicOr(&a.status->overflow, 1);
         return;
     }
-    // second pass: the same atoms, in the same order, straight into the j slots
     int* out = a.tile_j + (size_t)(tbase + nblock) * 32;
-    row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out);
+    if (natom <= kStageAtoms) {
+        for (int k = lane; k < natom; k += 32) out[k] = s_stage[w][k];
+    } else {
+        // second pass: the same atoms, in the same order, straight into the j slots
+        row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom);
+    }
     for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
     // pbc: some pair of an atom tile may need its own minimum image when the
     // cutoff sphere around block I reaches half a box length
