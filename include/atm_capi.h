@@ -72,7 +72,8 @@ extern "C" {
 #define ATM_RES_DW_DU0 13
 #define ATM_RES_DW_DW0 14
 #define ATM_RES_STATUS 15     /* device status word (0 = ok) */
-#define ATM_NUM_RES 16
+#define ATM_RES_DWDU 16       /* dW/du of the W actually computed (lambda2 fp when alpha = 0) */
+#define ATM_NUM_RES 17
 
 typedef struct atm_force_s* atm_force_t;
 typedef struct atm_nonbonded_s* atm_nonbonded_t;
@@ -197,6 +198,23 @@ int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_
 /* R x R matrix of beta * (e0_r + W_s(u_r)): replica r's coordinates under
  * replica s's alchemical parameters, from the last evaluation. */
 int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix);
+/* Per-replica displacement vectors (n x 3), as ATMMetaForce::setParticleParameters
+ * + updateParametersInContext (ATMMetaForce.cpp:26-40) for a batch replica. */
+int atm_batch_set_displacements(atm_batch_t b, int replica, const double* displ);
+/* Per-replica NonbondedForce charges, sigmas, epsilons (n each). */
+int atm_batch_set_nonbonded_parameters(atm_batch_t b, int replica, const double* charge, const double* sigma,
+                                       const double* epsilon);
+/* No counterpart in the reference (the adjoint of the ATM energy).  Gradients of
+ * L = sum_r g[r] W_r, W the softplus bias energy of the last evaluation, with
+ * respect to positions and displacements (sum n x 3), charges, sigmas, epsilons
+ * (sum n) and the 5 parameters lambda1, lambda2, alpha, u0, w0 (R x 5).  The
+ * batch must have been created with "Adjoint=1" for the charge/sigma/epsilon
+ * terms.  Device pointers on the given stream; every output is nullable. */
+int atm_batch_backward_device(atm_batch_t b, const double* d_g, double* d_dx, double* d_dd, double* d_dq,
+                              double* d_dsig, double* d_deps, double* d_dparams, void* stream);
+/* Same with host buffers. */
+int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, double* dq, double* dsig,
+                       double* deps, double* dparams);
 
 /* ---- allocation-free variant ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc:

@@ -12,9 +12,9 @@ import os
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "_build", "libatmgb300.so")
 
-NUM_RES = 16
+NUM_RES = 17
 RES_KEYS = ("energy", "pert", "sp", "W", "u", "e0", "bfp", "fp", "E1", "E2",
-            "dW_dlambda1", "dW_dlambda2", "dW_dalpha", "dW_du0", "dW_dw0", "status")
+            "dW_dlambda1", "dW_dlambda2", "dW_dalpha", "dW_du0", "dW_dw0", "status", "dW_du")
 
 ATM_ERRORS = {
     1: "invalid argument", 2: "index out of range", 3: "invalid state", 4: "CUDA failure",
@@ -97,6 +97,10 @@ _SIGS = {
     "atm_batch_evaluate": [_vp, _dp, _dp, _dp, _dp],
     "atm_batch_evaluate_device": [_vp, _vp, _vp, _vp, _vp],
     "atm_batch_energy_matrix": [_vp, C.c_double, _dp],
+    "atm_batch_set_displacements": [_vp, C.c_int, _dp],
+    "atm_batch_set_nonbonded_parameters": [_vp, C.c_int, _dp, _dp, _dp],
+    "atm_batch_backward_device": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "atm_batch_backward": [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
     "atm_batch_set_profiling": [_vp, C.c_int],
     "atm_batch_get_kernel_times": [_vp, C.c_char_p, _sz, _dp, C.c_int, _ip],
     "atm_batch_get_launch_count": [_vp, _ip],

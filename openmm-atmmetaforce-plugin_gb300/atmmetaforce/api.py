@@ -469,6 +469,36 @@ class ReplicaBatch:
         call("atm_batch_evaluate_device", self._h, C.c_void_p(d_pos), C.c_void_p(d_forces),
              C.c_void_p(d_results), C.c_void_p(stream))
 
+    def setDisplacements(self, replica, displ):
+        d = np.ascontiguousarray(np.asarray(displ, dtype=np.float64).reshape(-1, 3))
+        if len(d) != self.n[replica]:
+            raise ATMError(1, "wrong number of displacements")
+        call("atm_batch_set_displacements", self._h, int(replica), _ptr(d))
+
+    def setNonbondedParameters(self, replica, charge, sigma, epsilon):
+        q, s, e = (np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1)) for v in (charge, sigma, epsilon))
+        if not (len(q) == len(s) == len(e) == self.n[replica]):
+            raise ATMError(1, "wrong number of particle parameters")
+        call("atm_batch_set_nonbonded_parameters", self._h, int(replica), _ptr(q), _ptr(s), _ptr(e))
+
+    def backward(self, g=None):
+        """Gradients of sum_r g[r] W_r (g defaults to ones) from the last
+        evaluation: dict of positions, displacements (sum n, 3), charge, sigma,
+        epsilon (sum n) and params (R, 5: lambda1, lambda2, alpha, u0, w0)."""
+        g = np.ones(self.R) if g is None else np.ascontiguousarray(np.asarray(g, dtype=np.float64))
+        N = int(self.offsets[-1])
+        out = {"positions": np.zeros((N, 3)), "displacements": np.zeros((N, 3)), "charge": np.zeros(N),
+               "sigma": np.zeros(N), "epsilon": np.zeros(N), "params": np.zeros((self.R, 5))}
+        call("atm_batch_backward", self._h, _ptr(g), _ptr(out["positions"]), _ptr(out["displacements"]),
+             _ptr(out["charge"]), _ptr(out["sigma"]), _ptr(out["epsilon"]), _ptr(out["params"]))
+        return out
+
+    def backwardDevice(self, d_g, d_dx=0, d_dd=0, d_dq=0, d_dsig=0, d_deps=0, d_dpar=0, stream=0):
+        """Device-pointer variant of backward() (0 = output not wanted)."""
+        call("atm_batch_backward_device", self._h, C.c_void_p(d_g), C.c_void_p(d_dx or None),
+             C.c_void_p(d_dd or None), C.c_void_p(d_dq or None), C.c_void_p(d_dsig or None),
+             C.c_void_p(d_deps or None), C.c_void_p(d_dpar or None), C.c_void_p(stream or None))
+
     def energyMatrix(self, beta=1.0):
         M = np.zeros((self.R, self.R))
         call("atm_batch_energy_matrix", self._h, float(beta), _ptr(M))

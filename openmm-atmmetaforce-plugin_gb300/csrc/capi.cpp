@@ -47,6 +47,11 @@ struct atm_batch_s {
     std::vector<double> results;
     std::vector<double> matrix;
     bool evaluated = false;
+    double* scratch = nullptr;  // device staging of the host backward()
+    size_t scratch_n = 0;
+    ~atm_batch_s() {
+        if (scratch) cudaFree(scratch);
+    }
 };
 
 static thread_local std::string g_error;
@@ -581,13 +586,14 @@ int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, co
     REQUIRE(systems && out && n_replicas > 0, ATM_ERR_INVALID_ARGUMENT, "bad argument");
     auto props = parse_props(properties);
     bool diff = prop_bool(props, "DifferencePath", true);
+    bool adjoint = prop_bool(props, "Adjoint", false);
     std::vector<ReplicaSpec> v;
     for (int r = 0; r < n_replicas; r++) {
         REQUIRE(systems[r], ATM_ERR_INVALID_ARGUMENT, "null system");
         v.push_back(spec_from_system(systems[r]->sys));
     }
     std::unique_ptr<atm_batch_s> b(new atm_batch_s);
-    b->eng.reset(new Engine(std::move(v), device, !diff));
+    b->eng.reset(new Engine(std::move(v), device, !diff, adjoint));
     b->results.resize((size_t)NUM_RES * n_replicas);
     b->matrix.resize((size_t)n_replicas * n_replicas);
     *out = b.release();
@@ -655,6 +661,70 @@ int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_
     API_BEGIN
     REQUIRE(b && d_pos_all, ATM_ERR_INVALID_ARGUMENT, "null argument");
     b->eng->evaluate_device(d_pos_all, d_forces, d_results, (cudaStream_t)stream);
+    API_END
+}
+
+int atm_batch_set_displacements(atm_batch_t b, int replica, const double* displ) {
+    API_BEGIN
+    REQUIRE(b && displ, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    b->eng->set_displacements(replica, displ);
+    API_END
+}
+
+int atm_batch_set_nonbonded_parameters(atm_batch_t b, int replica, const double* charge, const double* sigma,
+                                       const double* epsilon) {
+    API_BEGIN
+    REQUIRE(b && charge && sigma && epsilon, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    b->eng->set_nonbonded_params(replica, charge, sigma, epsilon);
+    API_END
+}
+
+int atm_batch_backward_device(atm_batch_t b, const double* d_g, double* d_dx, double* d_dd, double* d_dq,
+                              double* d_dsig, double* d_deps, double* d_dparams, void* stream) {
+    API_BEGIN
+    REQUIRE(b && d_g, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    b->eng->backward(d_g, d_dx, d_dd, d_dq, d_dsig, d_deps, d_dparams, (cudaStream_t)stream);
+    API_END
+}
+
+int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, double* dq, double* dsig,
+                       double* deps, double* dparams) {
+    API_BEGIN
+    REQUIRE(b && g, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    const int R = b->eng->replicas(), n = b->eng->total_atoms();
+    // device staging, kept by the batch across calls
+    const size_t need = (size_t)R + 3 * (size_t)n * 2 + 3 * (size_t)n + 5 * (size_t)R;
+    if (b->scratch_n < need) {
+        if (b->scratch) cudaFree(b->scratch);
+        b->scratch = nullptr;
+        if (cudaMalloc(&b->scratch, need * sizeof(double)) != cudaSuccess) throw Error(ATM_ERR_CUDA, "cudaMalloc");
+        b->scratch_n = need;
+    }
+    double* dg = b->scratch;
+    double* ddx = dg + R;
+    double* ddd = ddx + 3 * (size_t)n;
+    double* ddq = ddd + 3 * (size_t)n;
+    double* dds = ddq + n;
+    double* dde = dds + n;
+    double* ddp = dde + n;
+    if (cudaMemcpy(dg, g, sizeof(double) * R, cudaMemcpyHostToDevice) != cudaSuccess)
+        throw Error(ATM_ERR_CUDA, "cudaMemcpy");
+    const bool adj = b->eng->adjoint();
+    b->eng->backward(dg, ddx, ddd, adj ? ddq : nullptr, adj ? dds : nullptr, adj ? dde : nullptr, ddp, 0);
+    auto get = [](double* h, const double* d, size_t k) {
+        if (h && cudaMemcpy(h, d, k * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+            throw Error(ATM_ERR_CUDA, "cudaMemcpy");
+    };
+    get(dx, ddx, 3 * (size_t)n);
+    get(dd, ddd, 3 * (size_t)n);
+    if (adj) {
+        get(dq, ddq, n);
+        get(dsig, dds, n);
+        get(deps, dde, n);
+    } else if (dq || dsig || deps) {
+        throw Error(ATM_ERR_STATE, "Charge/sigma/epsilon gradients need a batch created with Adjoint=1");
+    }
+    get(dparams, ddp, 5 * (size_t)R);
     API_END
 }
 

@@ -156,9 +156,10 @@ static double dispersion_coefficient(const ReplicaSpec& s) {
     return 8.0 * kPi * N * N * (sum1 / (9.0 * std::pow(s.cutoff, 9)) - sum2 / (3.0 * std::pow(s.cutoff, 3)));
 }
 
-Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode)
-    : R_((int)reps.size()), dev_(device), full_(full_mode), specs_(std::move(reps)) {
+Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool adjoint)
+    : R_((int)reps.size()), dev_(device), full_(full_mode), adjoint_(adjoint), specs_(std::move(reps)) {
     if (R_ <= 0) throw Error(1, "At least one replica is required");
+    if (adjoint_ && full_) throw Error(5, "The adjoint requires the difference path (DifferencePath=1)");
     const ReplicaSpec& s0 = specs_[0];
     method_ = s0.method;
     cutoff_ = s0.cutoff;
@@ -693,6 +694,9 @@ void Engine::alloc_device() {
     a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
     a.status = dalloc<Status>(d_allocs_, 1);
     a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);
+    a.adjoint = adjoint_ ? 1 : 0;
+    a.D = adjoint_ ? dalloc<unsigned long long>(d_allocs_, 3 * (size_t)NA_) : nullptr;
+    a.sqrt_ke = std::sqrt(kOne4PiEps0);
     a.n_exc = (int)exc_ij_.size();
     a.exc_ij = dupload(d_allocs_, exc_ij_);
     a.exc_p = dupload(d_allocs_, exc_p_);
@@ -968,5 +972,24 @@ void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_re
 }
 
 void Engine::reorder() { layout_ready_ = false; }
+
+void Engine::set_nonbonded_params(int r, const double* q, const double* sig, const double* eps) {
+    if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
+    ReplicaSpec& s = specs_[r];
+    std::memcpy(s.q.data(), q, sizeof(double) * (size_t)s.n);
+    std::memcpy(s.sig.data(), sig, sizeof(double) * (size_t)s.n);
+    std::memcpy(s.eps.data(), eps, sizeof(double) * (size_t)s.n);
+    layout_ready_ = false;  // scaled charges, LJ pairs, exception charges and self energy follow
+}
+
+void Engine::backward(const double* d_g, double* d_dx, double* d_dd, double* d_dq, double* d_dsig, double* d_deps,
+                      double* d_dpar, cudaStream_t stream) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    if (!layout_ready_) throw Error(3, "backward() needs a preceding evaluation");
+    if (!adjoint_ && (d_dq || d_dsig || d_deps))
+        throw Error(3, "Charge/sigma/epsilon gradients need a batch created with Adjoint=1");
+    launch_adjoint(A_, d_g, d_dx, d_dd, d_dq, d_dsig, d_deps, d_dpar, stream);
+    CUDA_CHECK(cudaGetLastError());
+}
 
 }  // namespace atm

@@ -39,7 +39,8 @@ struct KernelTime {
 
 class Engine {
 public:
-    Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode);
+    // adjoint: also accumulate the derivatives needed by backward() (difference mode only)
+    Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool adjoint = false);
     ~Engine();
     Engine(const Engine&) = delete;
     Engine& operator=(const Engine&) = delete;
@@ -66,6 +67,14 @@ public:
     // Re-sort atoms from the current positions (exclusion masks follow).
     void reorder();
 
+    // New charges, sigmas and epsilons of one replica's NonbondedForce (n each).
+    void set_nonbonded_params(int r, const double* q, const double* sig, const double* eps);
+    bool adjoint() const { return adjoint_; }
+    // Gradients of sum_r g[r] W_r from the last evaluation (device pointers on
+    // the given stream; outputs nullable, user order).
+    void backward(const double* d_g, double* d_dx, double* d_dd, double* d_dq, double* d_dsig, double* d_deps,
+                  double* d_dpar, cudaStream_t stream);
+
     void set_profiling(bool on) { profiling_ = on; }
     const std::vector<KernelTime>& kernel_times() const { return times_; }
     int launches_per_eval() const;
@@ -90,6 +99,7 @@ private:
 
     int R_ = 0, dev_ = 0;
     bool full_ = false;
+    bool adjoint_ = false;
     std::vector<ReplicaSpec> specs_;
     std::vector<int> in_off_;
     int n_in_ = 0;

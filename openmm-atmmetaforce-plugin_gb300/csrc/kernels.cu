@@ -82,6 +82,8 @@ __global__ void k_prepare(Args a) {
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
     for (int k = 0; k < 6; k++) a.F[(size_t)k * a.NA + s] = 0ull;
+    if (a.adjoint)
+        for (int k = 0; k < 3; k++) a.D[(size_t)k * a.NA + s] = 0ull;
     warp_bbox(x, y, z, R, &a.bb_c[b], &a.bb_h[b], lane, nreal);
     if (a.full) {
         float4 d = a.displ[s];
@@ -112,8 +114,11 @@ void launch_prepare(const Args& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // exceptions: FP64, user-order positions; one CTA per 256 exceptions of a replica
 // ---------------------------------------------------------------------------
+// One exception pair at separation (dx, dy, dz): energy, force on j (f), and
+// (gcorr) erf(alpha r)/r of its Ewald exclusion correction.
 __device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const ExcParam& p, double dx, double dy,
-                                           double dz, double* f) {
+                                           double dz, double* f, double* gcorr) {
+    *gcorr = 0.0;
     double r2 = dx * dx + dy * dy + dz * dz;
     double e = 0.0, fr = 0.0;
     if (p.x != 0.0 || p.z != 0.0) {
@@ -142,12 +147,14 @@ __device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const
             double ar = a.alphad * r;
             double ef = erf(ar);
             e -= p.w * ef / r;
+            *gcorr = ef / r;
             double fm = p.w * (1.1283791670955126 * a.alphad * exp(-ar * ar) - ef / r) / m2;
             f[0] += fm * mx;
             f[1] += fm * my;
             f[2] += fm * mz;
         } else {
             e -= p.w * 1.1283791670955126 * a.alphad;
+            *gcorr = 1.1283791670955126 * a.alphad;
         }
     }
     return e;
@@ -167,19 +174,24 @@ __global__ void __launch_bounds__(256) k_exceptions(Args a) {
         const double* di = a.displ_in + 3 * (size_t)ij.x;
         const double* dj = a.displ_in + 3 * (size_t)ij.y;
         int si = a.slot_of[ij.x], sj = a.slot_of[ij.y];
-        double f1[3], f2[3];
-        E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1);
+        double f1[3], f2[3], g1, g2;
+        E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1, &g1);
         for (int k = 0; k < 3; k++) {
             fix_add_d(a.F + (size_t)k * a.NA + si, -f1[k]);
             fix_add_d(a.F + (size_t)k * a.NA + sj, f1[k]);
         }
         if (a.full || ij.w) {
             E2 = exc_term(a, R, p, (xj[0] + dj[0]) - (xi[0] + di[0]), (xj[1] + dj[1]) - (xi[1] + di[1]),
-                          (xj[2] + dj[2]) - (xi[2] + di[2]), f2);
+                          (xj[2] + dj[2]) - (xi[2] + di[2]), f2, &g2);
             if (!a.full) {
                 DE = E2 - E1;
                 E2 = 0.0;
                 for (int k = 0; k < 3; k++) f2[k] -= f1[k];
+                if (a.adjoint) {
+                    // the exclusion correction -q_i q_j erf(alpha r)/r in scaled charges
+                    fix_add_d(a.D + si, -(double)a.qs[sj] * (g2 - g1));
+                    fix_add_d(a.D + sj, -(double)a.qs[si] * (g2 - g1));
+                }
             }
             for (int k = 0; k < 3; k++) {
                 fix_add_d(a.F + (size_t)(3 + k) * a.NA + si, -f2[k]);
@@ -518,7 +530,8 @@ void launch_conv(const Args& a, cudaStream_t s) {
 }
 
 __device__ __forceinline__ void gather_one(const float* G, const RepDev& R, const Stencil& S, float& gx, float& gy,
-                                           float& gz) {
+                                           float& gz, float* pot = nullptr) {
+    float ph = 0.f;
     const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
     int iz[5];
 #pragma unroll
@@ -546,14 +559,17 @@ __device__ __forceinline__ void gather_one(const float* G, const RepDev& R, cons
             gx += S.dw[0][a0] * S.w[1][b0] * sx;
             gy += S.w[0][a0] * S.dw[1][b0] * sx;
             gz += S.w[0][a0] * S.w[1][b0] * sz;
+            if (pot) ph += S.w[0][a0] * S.w[1][b0] * sx;
         }
     }
+    if (pot) *pot = ph;
 }
 
 // Gradients of two grids at one stencil (the state-1 potential and the
 // potential of the moved charges).
 __device__ __forceinline__ void gather_two(const float* G1, const float* G2, const RepDev& R, const Stencil& S,
-                                           float* g1, float* g2) {
+                                           float* g1, float* g2, float* pot2 = nullptr) {
+    float ph2 = 0.f;
     const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
     int iz[5];
 #pragma unroll
@@ -588,8 +604,10 @@ __device__ __forceinline__ void gather_two(const float* G1, const float* G2, con
             g2[0] += dxy * s2;
             g2[1] += xdy * s2;
             g2[2] += xy * z2;
+            if (pot2) ph2 += xy * s2;
         }
     }
+    if (pot2) *pot2 = ph2;
 }
 
 __device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, int s, float q, float gx, float gy,
@@ -625,10 +643,11 @@ __global__ void __launch_bounds__(128, 6) k_gather(Args a) {
         add_grad_force(F2, a.NA, s, p.w, gx, gy, gz, R);
     } else {
         // F1 from the state-1 potential; F2 - F1 from the potential of the moved charges
-        float g1[3], g2[3];
-        gather_two(phi1, phi2, R, S, g1, g2);
+        float g1[3], g2[3], pot2 = 0.f;
+        gather_two(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr);
         add_grad_force(a.F, a.NA, s, p.w, g1[0], g1[1], g1[2], R);
         add_grad_force(F2, a.NA, s, p.w, g2[0], g2[1], g2[2], R);
+        if (a.adjoint) fix_add(a.D + s, pot2);  // d(E2 - E1)_rec / d(scaled charge)
     }
 }
 
@@ -647,15 +666,16 @@ __global__ void k_gather_moving(Args a) {
     const float* phi2 = phi1 + G3;
     Stencil S;
     make_stencil(p.x, p.y, p.z, R, S, true);
-    float gx, gy, gz, hx, hy, hz, kx, ky, kz;
-    gather_one(phi1, R, S, gx, gy, gz);
+    float gx, gy, gz, hx, hy, hz, kx, ky, kz, pg, ph, pk;
+    gather_one(phi1, R, S, gx, gy, gz, &pg);
     add_grad_force(a.F, a.NA, s, p.w, gx, gy, gz, R);
     const float4 d = a.displ[s];
     make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
                  wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
-    gather_one(phi1, R, S, hx, hy, hz);
-    gather_one(phi2, R, S, kx, ky, kz);
+    gather_one(phi1, R, S, hx, hy, hz, &ph);
+    gather_one(phi2, R, S, kx, ky, kz, &pk);
     add_grad_force(a.F + 3 * (size_t)a.NA, a.NA, s, p.w, hx + kx - gx, hy + ky - gy, hz + kz - gz, R);
+    if (a.adjoint) fix_add(a.D + s, ph + pk - pg);  // potential at x + d in state 2 minus at x in state 1
 }
 
 void launch_gather(const Args& a, cudaStream_t s) {
@@ -719,6 +739,9 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
         out[RES_DU0] = 0.0;
     }
     out[RES_DW0] = 1.0;
+    // derivative of the W computed above (with alpha = 0 the log term is absent, so
+    // dW/dusc = lambda2, not the bfp the force merge uses)
+    out[RES_DWDU] = (alpha > 0 ? bfp : l2) * fp;
 }
 
 __device__ double block_sum(double v, double* sh) {
@@ -826,6 +849,48 @@ __global__ void k_matrix(Args a) {
 void launch_matrix(const Args& a, cudaStream_t s) {
     int n = a.R * a.R;
     k_matrix<<<(n + 127) / 128, 128, 0, s>>>(a);
+}
+
+// Backward pass of L = sum_r g_r W_r from the last (adjoint) evaluation.  With
+// s = +1 for direction > 0 (u = U2 - U1) and -1 otherwise:
+//   dW/dx = -s W'(u) (F2 - F1),  dW/dd = -s W'(u) F2,
+//   dW/d{q, sigma, eps} = s W'(u) d(U2 - U1)/d{q, sigma, eps}.
+__global__ void k_adjoint(Args a, const double* g, double* dx, double* dd, double* dq, double* dsig, double* deps,
+                          double* dpar) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.R * 5 && dpar) {
+        const int r = s / 5, k = s % 5;
+        dpar[s] = g[r] * a.results[(size_t)r * NUM_RES + RES_DL1 + k];
+    }
+    if (s >= a.NA) return;
+    const int o = a.orig[s];
+    if (o < 0) return;
+    const int rep = a.block_rep[s >> 5];
+    const RepDev& R = a.reps[rep];
+    const double* res = a.results + (size_t)rep * NUM_RES;
+    const double sgn = R.params[8] > 0 ? 1.0 : -1.0;
+    const double w = R.var_nb ? g[rep] * res[RES_DWDU] : 0.0;
+    const size_t u = (size_t)(R.in_off + o);
+    const double sc = 1.0 / kFixScale;
+    for (int k = 0; k < 3; k++) {
+        const long long f1 = (long long)a.F[(size_t)k * a.NA + s];
+        const long long f2 = (long long)a.F[(size_t)(3 + k) * a.NA + s];
+        const double delta = a.full ? (double)(f2 - f1) : (double)f2;  // F2 - F1
+        if (dx) dx[3 * u + k] = -sgn * w * delta * sc;
+        if (dd) dd[3 * u + k] = -sgn * w * ((double)f1 + delta) * sc;
+    }
+    if (a.adjoint) {
+        const double dqs = (double)(long long)a.D[s] * sc;
+        if (dq) dq[u] = sgn * w * dqs * (double)a.sqrt_ke;
+        if (dsig) dsig[u] = sgn * w * (double)(long long)a.D[a.NA + s] * sc;
+        if (deps) deps[u] = sgn * w * (double)(long long)a.D[2 * (size_t)a.NA + s] * sc;
+    }
+}
+
+void launch_adjoint(const Args& a, const double* g, double* dx, double* dd, double* dq, double* dsig, double* deps,
+                    double* dpar, cudaStream_t s) {
+    int n = a.NA > 5 * a.R ? a.NA : 5 * a.R;
+    k_adjoint<<<(n + 255) / 256, 256, 0, s>>>(a, g, dx, dd, dq, dsig, deps, dpar);
 }
 
 }  // namespace atm

@@ -24,7 +24,7 @@ enum RowKind { ROW_STATE1 = 0, ROW_STATE2 = 1, ROW_DIFF1 = 2, ROW_DIFF2 = 3 };
 // Result record layout (matches ATM_RES_* in include/atm_capi.h).
 enum Res {
     RES_ENERGY = 0, RES_PERT, RES_SP, RES_W, RES_U, RES_E0, RES_BFP, RES_FP, RES_E1, RES_E2,
-    RES_DL1, RES_DL2, RES_DALPHA, RES_DU0, RES_DW0, RES_STATUS, NUM_RES
+    RES_DL1, RES_DL2, RES_DALPHA, RES_DU0, RES_DW0, RES_STATUS, RES_DWDU, NUM_RES
 };
 
 // Per-replica constants and offsets (device copy refreshed every evaluation).
@@ -116,6 +116,11 @@ struct Args {
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]
     unsigned long long* F;
+    // adjoint (difference mode): planes of NA of d(U2-U1)/d(q*sqrt(ke)), d/dsigma,
+    // d/depsilon, int64 fixed point; null when the adjoint is off
+    int adjoint;
+    unsigned long long* D;
+    double sqrt_ke;
     // exceptions (user-order indices, grouped by replica)
     int n_exc;
     const int4* exc_ij;       // (i_in, j_in, replica, cross)
@@ -151,6 +156,11 @@ void launch_gather(const Args& a, cudaStream_t s);
 void launch_finalize(const Args& a, cudaStream_t s);
 void launch_output(const Args& a, cudaStream_t s);
 void launch_matrix(const Args& a, cudaStream_t s);
+// Gradients of sum_r g_r W_r (host-provided upstream gradient g, device array of R):
+// positions, displacements, charges, sigmas, epsilons (user order, n_in each; x3 for
+// vectors) and the 5 softplus parameters per replica (R x 5).  Outputs nullable.
+void launch_adjoint(const Args& a, const double* g, double* dx, double* dd, double* dq, double* dsig, double* deps,
+                    double* dpar, cudaStream_t s);
 int tiles_kernel_blocks_per_sm();
 constexpr int kTileThreads = 256;
 

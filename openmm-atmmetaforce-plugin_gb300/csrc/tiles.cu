@@ -278,8 +278,71 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
     }
 }
 
+// Difference tiles with the adjoint: besides energy and forces, the derivatives
+// of the pair energy with respect to each partner's scaled charge, sigma and
+// epsilon (LJ: dphi/dsigma_i = eps4 (6 s^12 - 3 s^6) / sigma_ij,
+// dphi/deps_i = phi_LJ / (2 eps_i)); j-side sums travel with their slot.
+template <int METHOD, bool PBC>
+__device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
+                                               float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
+                                               float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
+                                               float crf, float3& fi, float3& fj, double& e64, float3& ai,
+                                               float3& aj) {
+    const int src = (lane + 1) & 31;
+    const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
+#pragma unroll 4
+    for (int k = 0; k < 32; k++) {
+        const int jl = (lane + k) & 31;
+        const float4 pj = sp[jl];
+        const float2 lj = sl[jl];
+        float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        if (PBC) {
+            dx = min_img(dx, Lx, iLx);
+            dy = min_img(dy, Ly, iLy);
+            dz = min_img(dz, Lz, iLz);
+        }
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const bool inc = ((mask >> k) & 1u) && r2 < rc2;
+        const float r2s = inc ? r2 : 1.0f;
+        const float invr = rsqrtf(r2s), invr2 = invr * invr;
+        const float sig = li.x + lj.x;
+        const float s2 = sig * sig * invr2, s6 = s2 * s2 * s2;
+        const float t6 = (li.y * lj.y) * s6;
+        const float elj = t6 * s6 - t6;
+        const float dsg = sig > 0.f ? (6.0f * t6 * s6 - 3.0f * t6) / sig : 0.f;
+        float fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
+        float gq;
+        if (METHOD == 4) {
+            const float ar = alpha * r2s * invr;
+            const float ex = __expf(-ar * ar);
+            gq = erfc_as(ar, ex) * invr;
+            fr += pi.w * pj.w * (gq + 1.1283791670955126f * alpha * ex) * invr2;
+        } else {
+            gq = invr + krf * r2s - crf;
+            fr += pi.w * pj.w * (invr * invr2 - 2.0f * krf);
+        }
+        const float on = inc ? 1.0f : 0.0f;
+        e64 += (double)(on * (elj + pi.w * pj.w * gq));
+        fr *= on;
+        const float inv_ej = lj.y > 0.f ? 2.0f / (lj.y * lj.y) : 0.f;
+        ai.x += on * gq * pj.w;
+        ai.y += on * dsg;
+        ai.z += on * elj * inv_ei;
+        const float fx = fr * dx, fy = fr * dy, fz = fr * dz;
+        fi.x -= fx;
+        fi.y -= fy;
+        fi.z -= fz;
+        fj.x = __shfl_sync(FULL_MASK, fj.x + fx, src);
+        fj.y = __shfl_sync(FULL_MASK, fj.y + fy, src);
+        fj.z = __shfl_sync(FULL_MASK, fj.z + fz, src);
+        aj.x = __shfl_sync(FULL_MASK, aj.x + on * gq * pi.w, src);
+        aj.y = __shfl_sync(FULL_MASK, aj.y + on * dsg, src);
+        aj.z = __shfl_sync(FULL_MASK, aj.z + on * elj * inv_ej, src);
+    }
+}
+
 template <int METHOD>
-__global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
+__global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     __shared__ float4 s_p[kTileThreads / 32][32];
     __shared__ float2 s_l[kTileThreads / 32][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -343,9 +406,18 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
         s_l[w][lane] = lj;
         __syncwarp();
         float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
+        float3 ai = make_float3(0.f, 0.f, 0.f), aj = make_float3(0.f, 0.f, 0.f);
         float e32 = 0.f;
         double e64 = 0.0;
-        if (diff) {
+        const bool adj = diff && a.adjoint;
+        if (adj) {
+            if (pbc)
+                tile_steps_adj<METHOD, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                             alpha, krf, crf, fi, fj, e64, ai, aj);
+            else
+                tile_steps_adj<METHOD, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                              alpha, krf, crf, fi, fj, e64, ai, aj);
+        } else if (diff) {
             if (pbc)
                 tile_steps<METHOD, true, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
                                                alpha, krf, crf, fi, fj, e32, e64);
@@ -375,6 +447,17 @@ __global__ void __launch_bounds__(kTileThreads) k_tiles(Args a) {
             fix_add_t(Fp + j, sign * fj.x);
             fix_add_t(Fp + a.NA + j, sign * fj.y);
             fix_add_t(Fp + 2 * (size_t)a.NA + j, sign * fj.z);
+        }
+        if (adj) {
+            unsigned long long* D = a.D;
+            fix_add_t(D + i, sign * ai.x);
+            fix_add_t(D + a.NA + i, sign * ai.y);
+            fix_add_t(D + 2 * (size_t)a.NA + i, sign * ai.z);
+            if (jvalid) {
+                fix_add_t(D + j, sign * aj.x);
+                fix_add_t(D + a.NA + j, sign * aj.y);
+                fix_add_t(D + 2 * (size_t)a.NA + j, sign * aj.z);
+            }
         }
     }
 }
