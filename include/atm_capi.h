@@ -239,6 +239,15 @@ int atm_rf_nonbonded_noalloc(int n, const double* d_pos, const double* d_charge,
                              const double* d_epsilon, const int* d_excl_start, const int* d_excl, const double* box,
                              double cutoff, double eps_rf, double* d_energy, double* d_forces, void* stream);
 
+/* ---- autotuner -------------------------------------------------------------- */
+/* No counterpart in the reference.  Times `trials` evaluations per configuration
+ * of the launch space (pair-tile CTAs per SM, PME spreading brick edge 8/12/16,
+ * PME chain on its own stream or in line) on the stored positions and keeps the
+ * fastest; with use_cache a choice stored for the same GPU and workload (file
+ * $ATM_AUTOTUNE_CACHE, else ~/.cache/atm_gb300_autotune.txt) is reused.  The
+ * report (one line per configuration) is written to report (nullable). */
+int atm_batch_autotune(atm_batch_t b, int trials, int use_cache, char* report, size_t cap, size_t* len);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Timings (ms) of the kernels of the last evaluate() when profiling is on. */
 int atm_batch_set_profiling(atm_batch_t b, int on);

@@ -102,6 +102,7 @@ _SIGS = {
     "atm_batch_backward_device": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "atm_batch_backward": [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
     "atm_batch_set_profiling": [_vp, C.c_int],
+    "atm_batch_autotune": [_vp, C.c_int, C.c_int, C.c_char_p, _sz, C.POINTER(_sz)],
     "atm_batch_get_kernel_times": [_vp, C.c_char_p, _sz, _dp, C.c_int, _ip],
     "atm_batch_get_launch_count": [_vp, _ip],
     "atm_batch_get_stats": [_vp, _ip, _ip, _ip],

@@ -504,6 +504,14 @@ class ReplicaBatch:
         call("atm_batch_energy_matrix", self._h, float(beta), _ptr(M))
         return M
 
+    def autotune(self, trials=5, use_cache=True):
+        """Time the launch space on the stored positions and keep the fastest
+        configuration; returns the report."""
+        buf = C.create_string_buffer(8192)
+        n = C.c_size_t()
+        call("atm_batch_autotune", self._h, int(trials), int(bool(use_cache)), buf, 8192, C.byref(n))
+        return buf.value.decode()
+
     def setProfiling(self, on):
         call("atm_batch_set_profiling", self._h, int(bool(on)))
 

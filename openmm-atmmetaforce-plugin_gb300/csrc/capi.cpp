@@ -736,6 +736,15 @@ int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix) {
     API_END
 }
 
+int atm_batch_autotune(atm_batch_t b, int trials, int use_cache, char* report, size_t cap, size_t* len) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    REQUIRE(trials > 0, ATM_ERR_INVALID_ARGUMENT, "trials must be positive");
+    std::string rep = b->eng->autotune(trials, use_cache != 0);
+    copy_string(rep, report, cap, len);
+    API_END
+}
+
 int atm_batch_set_profiling(atm_batch_t b, int on) {
     API_BEGIN
     REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");

@@ -10,6 +10,8 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cstdlib>
+#include <fstream>
 #include <array>
 #include <cmath>
 #include <cstring>
@@ -202,11 +204,12 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     CUDA_CHECK(cudaMallocHost(&h_beta_, sizeof(double)));
     CUDA_CHECK(cudaMallocHost(&h_status_, sizeof(Status)));
     std::memset(h_pos_, 0, sizeof(double) * 3 * (size_t)n_in_);
-    int sms = 0, per = 0;
-    CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
+    int per = 0;
+    CUDA_CHECK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev_));
     per = tiles_kernel_blocks_per_sm();
     if (per < 1) per = 1;
-    tile_grid_ = sms * per;
+    max_tile_per_sm_ = per;
+    tile_grid_ = sms_ * per;
 }
 
 Engine::~Engine() {
@@ -566,20 +569,7 @@ void Engine::build_layout() {
                 for (double v : m) moduli_.push_back((float)v);
             }
         }
-        // spreading bricks: at most 16 grid points per dimension, two grids per replica
-        brick_cta_rep_.clear();
-        brick_smem_ = 0;
-        for (int r = 0; r < R_; r++) {
-            RepDev& rd = rep_host_[r];
-            for (int d = 0; d < 3; d++) {
-                rd.nbrick[d] = (rd.K[d] + 15) / 16;
-                rd.bsz[d] = (rd.K[d] + rd.nbrick[d] - 1) / rd.nbrick[d];
-            }
-            rd.brick_cta_b = (int)brick_cta_rep_.size();
-            int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
-            for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
-            brick_smem_ = std::max(brick_smem_, (int)(sizeof(unsigned long long) * rd.bsz[0] * rd.bsz[1] * rd.bsz[2]));
-        }
+        build_bricks();
         for (int r = 0; r < R_; r++) {
             RepDev& rd = rep_host_[r];
             long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
@@ -603,6 +593,124 @@ void Engine::build_layout() {
     }
     if (tile_cap_ == 0) tile_cap_ = nrows_ * 28 + 4096;
     layout_ready_ = true;
+}
+
+// Spreading bricks: at most tune_brick_ grid points per dimension, two grids per replica.
+void Engine::build_bricks() {
+    brick_cta_rep_.clear();
+    brick_smem_ = 0;
+    for (int r = 0; r < R_; r++) {
+        RepDev& rd = rep_host_[r];
+        for (int d = 0; d < 3; d++) {
+            rd.nbrick[d] = (rd.K[d] + tune_brick_ - 1) / tune_brick_;
+            rd.bsz[d] = (rd.K[d] + rd.nbrick[d] - 1) / rd.nbrick[d];
+        }
+        rd.brick_cta_b = (int)brick_cta_rep_.size();
+        int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
+        for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
+        brick_smem_ = std::max(brick_smem_, (int)(sizeof(unsigned long long) * rd.bsz[0] * rd.bsz[1] * rd.bsz[2]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: times the evaluation graph over pair-tile residency, spreading
+// brick size and PME stream overlap; keeps the fastest (cached per workload).
+// ---------------------------------------------------------------------------
+
+std::string Engine::tuning_key() const {
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, dev_);
+    std::ostringstream k;
+    k << prop.name << "|R" << R_ << "|N" << n_in_ << "|m" << method_ << "|rc" << cutoff_ << "|full" << full_
+      << "|adj" << adjoint_;
+    if (!rep_host_.empty()) k << "|K" << rep_host_[0].K[0] << "x" << rep_host_[0].K[1] << "x" << rep_host_[0].K[2];
+    return k.str();
+}
+
+void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream) {
+    bool rebuild = brick != tune_brick_;
+    tune_tile_per_sm_ = tile_per_sm;
+    tune_brick_ = brick;
+    tune_pme_stream_ = pme_stream;
+    tile_grid_ = sms_ * std::min(std::max(1, tile_per_sm), max_tile_per_sm_);
+    if (rebuild && layout_ready_ && method_ == NonbondedForce::PME) {
+        build_bricks();
+        alloc_device();
+    }
+    destroy_graphs();
+}
+
+static std::string cache_path() {
+    const char* p = std::getenv("ATM_AUTOTUNE_CACHE");
+    if (p && *p) return p;
+    const char* x = std::getenv("XDG_CACHE_HOME");
+    const char* h = std::getenv("HOME");
+    if (x && *x) return std::string(x) + "/atm_gb300_autotune.txt";
+    if (h && *h) return std::string(h) + "/.cache/atm_gb300_autotune.txt";
+    return "atm_gb300_autotune.txt";
+}
+
+bool Engine::load_tuning() {
+    std::ifstream f(cache_path());
+    std::string line, key = tuning_key();
+    while (std::getline(f, line)) {
+        auto tab = line.find('\t');
+        if (tab == std::string::npos || line.substr(0, tab) != key) continue;
+        std::istringstream v(line.substr(tab + 1));
+        int t, b, s;
+        if (v >> t >> b >> s) {
+            apply_tuning(t, b, s != 0);
+            return true;
+        }
+    }
+    return false;
+}
+
+std::string Engine::autotune(int trials, bool use_cache) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    if (!layout_ready_) {
+        build_layout();
+        alloc_device();
+    }
+    if (use_cache && load_tuning()) return "cached: " + tuning_key();
+    std::ostringstream rep;
+    double best = 1e30;
+    int bt = max_tile_per_sm_, bb = tune_brick_;
+    bool bs = tune_pme_stream_;
+    const bool pme = method_ == NonbondedForce::PME;
+    std::vector<int> bricks = pme ? std::vector<int>{16, 12, 8} : std::vector<int>{tune_brick_};
+    std::vector<int> pmes = pme ? std::vector<int>{1, 0} : std::vector<int>{1};
+    cudaEvent_t e0, e1;
+    CUDA_CHECK(cudaEventCreate(&e0));
+    CUDA_CHECK(cudaEventCreate(&e1));
+    for (int t = max_tile_per_sm_; t >= 2 && t >= max_tile_per_sm_ - 2; t--)
+        for (int b : bricks)
+            for (int s : pmes) {
+                apply_tuning(t, b, s != 0);
+                run(true, nullptr, nullptr);   // uploads the staged positions (buffers may be new)
+                run(false, nullptr, nullptr);  // device graph capture + one warm evaluation
+                CUDA_CHECK(cudaEventRecord(e0, s_main_));
+                for (int k = 0; k < trials; k++) CUDA_CHECK(cudaGraphLaunch(graph_dev_, s_main_));
+                CUDA_CHECK(cudaEventRecord(e1, s_main_));
+                CUDA_CHECK(cudaEventSynchronize(e1));
+                float ms = 0;
+                CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+                ms /= trials;
+                rep << "tiles/SM=" << t << " brick=" << b << " pme_stream=" << s << " : " << ms << " ms\n";
+                if (ms < best) {
+                    best = ms;
+                    bt = t;
+                    bb = b;
+                    bs = s != 0;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply_tuning(bt, bb, bs);
+    rep << "chosen: tiles/SM=" << bt << " brick=" << bb << " pme_stream=" << bs << " (" << best << " ms)\n";
+    std::ofstream f(cache_path(), std::ios::app);
+    if (f) f << tuning_key() << "\t" << bt << " " << bb << " " << (bs ? 1 : 0) << "\n";
+    return rep.str();
 }
 
 // ---------------------------------------------------------------------------
@@ -786,21 +894,30 @@ void Engine::record(cudaStream_t st, bool host_io) {
     launch_prepare(a, st);
     bool pme = method_ == NonbondedForce::PME;
     if (pme) {
-        CUDA_CHECK(cudaEventRecord(ev_fork_, st));
-        CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork_, 0));
-        launch_spread(a, s_pme_);
+        // the PME chain on its own stream (overlapping the pair tiles) or in line,
+        // as the autotuner chose
+        cudaStream_t ps = tune_pme_stream_ ? s_pme_ : st;
+        if (tune_pme_stream_) {
+            CUDA_CHECK(cudaEventRecord(ev_fork_, st));
+            CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork_, 0));
+        }
+        for (auto& g : groups_) {
+            CUFFT_CHECK(cufftSetStream(g.fwd, ps));
+            CUFFT_CHECK(cufftSetStream(g.inv, ps));
+        }
+        launch_spread(a, ps);
         for (auto& g : groups_)
             CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
-        launch_conv(a, s_pme_);
+        launch_conv(a, ps);
         for (auto& g : groups_)
             CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
-        launch_gather(a, s_pme_);
-        CUDA_CHECK(cudaEventRecord(ev_join_, s_pme_));
+        launch_gather(a, ps);
+        if (tune_pme_stream_) CUDA_CHECK(cudaEventRecord(ev_join_, s_pme_));
     }
     launch_find(a, st);
     launch_tiles(a, tile_grid_, st);
     launch_exceptions(a, st);
-    if (pme) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
+    if (pme && tune_pme_stream_) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
     launch_finalize(a, st);
     launch_output(a, st);
     launch_matrix(a, st);

@@ -75,6 +75,11 @@ public:
     void backward(const double* d_g, double* d_dx, double* d_dd, double* d_dq, double* d_dsig, double* d_deps,
                   double* d_dpar, cudaStream_t stream);
 
+    // Times the evaluation over the tuning space (pair-tile CTAs per SM, PME
+    // spreading brick size, PME stream overlap) and keeps the fastest; with
+    // use_cache, a stored choice for the same GPU and workload is reused.
+    // Returns a report.  Needs positions.
+    std::string autotune(int trials, bool use_cache);
     void set_profiling(bool on) { profiling_ = on; }
     const std::vector<KernelTime>& kernel_times() const { return times_; }
     int launches_per_eval() const;
@@ -87,6 +92,10 @@ public:
 
 private:
     void build_layout();
+    void build_bricks();
+    std::string tuning_key() const;
+    void apply_tuning(int tile_per_sm, int brick, bool pme_stream);
+    bool load_tuning();
     void alloc_device();
     void free_device();
     void upload_static();
@@ -113,6 +122,10 @@ private:
     bool layout_ready_ = false;
     bool profiling_ = false;
     int tile_grid_ = 0;
+    int sms_ = 0, max_tile_per_sm_ = 1;
+    int tune_tile_per_sm_ = 0;     // 0: as many as fit
+    int tune_brick_ = 16;          // spreading brick edge (grid points)
+    bool tune_pme_stream_ = true;  // PME on its own stream
 
     // host copies of the layout
     std::vector<int> orig_, slot_of_, block_rep_, block_cls_;

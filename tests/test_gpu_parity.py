@@ -88,6 +88,24 @@ def test_pme_23558(diff):
     check_case(S.abfe_pme_23558(1), diff)
 
 
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_rbfe_two_ligands_60000(diff):
+    """Relative swap: ligand A displaced +(2.5,2.5,2.5), ligand B -(2.5,2.5,2.5);
+    the difference path must also count the A x B pairs, which move relative to
+    each other."""
+    check_case(S.rbfe_pme_60000(), diff)
+
+
+def test_mixed_batch_of_eight_uneven_boxes():
+    cases = S.mixed_batch_8()
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    E, F, res = b.evaluate(np.concatenate([c.pos for c in cases]))
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        assert abs(res[k]["pert"] - ref["usc"]) <= U_TOL, k
+        assert force_rel(F[b.offsets[k]:b.offsets[k + 1]], ref["forces"]) <= F_TOL, k
+
+
 def test_deterministic_bitwise():
     c = S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=12)
     sys_, nb, f = atm.system_from_case(c)
@@ -124,6 +142,25 @@ def test_batch_mixed_sizes_vs_oracle_and_matrix():
             m = O.atm_merge(refs[r]["E1"], refs[r]["E2"], cases[s].params)
             tol = 0.4 * (energy_tol(cases[r].spec, cases[r].pos) + U_TOL)
             assert abs(M[r, s] - 0.4 * m["energy"]) <= tol
+
+
+def test_autotune_keeps_parity(tmp_path, monkeypatch):
+    monkeypatch.setenv("ATM_AUTOTUNE_CACHE", str(tmp_path / "tune.txt"))
+    cases = [S.abfe_pme_small(3000, 14, 81), S.abfe_pme_small(3000, 14, 82)]
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    pos = np.concatenate([c.pos for c in cases])
+    E0, F0, r0 = b.evaluate(pos)
+    report = b.autotune(trials=2, use_cache=False)
+    assert "chosen:" in report and report.count("ms") >= 3
+    E1, F1, r1 = b.evaluate(pos)
+    np.testing.assert_allclose(F1, F0, rtol=0, atol=1e-5)
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        assert abs(r1[k]["pert"] - ref["usc"]) <= U_TOL
+    # a second batch of the same workload reuses the stored choice
+    b2 = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    b2.evaluate(pos)
+    assert b2.autotune(trials=2, use_cache=True).startswith("cached")
 
 
 def test_batch_matches_single_contexts():
