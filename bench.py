@@ -39,6 +39,8 @@ def parse():
     p.add_argument("--replicas", type=int, default=22)
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--tune-cache", action="store_true",
+                   help="reuse a stored autotuning choice for this GPU and workload (profiling runs)")
     return p.parse_args()
 
 
@@ -219,7 +221,7 @@ def main():
     pos_host = np.ascontiguousarray(np.concatenate([c.pos for c in cases]))
     batch = atm.ReplicaBatch(systems, local, {"DifferencePath": 1})
     batch.evaluate(pos_host)  # layout + capacity
-    tune_report = batch.autotune(trials=5, use_cache=False)  # set-up, outside the timed region
+    tune_report = batch.autotune(trials=5, use_cache=args.tune_cache)  # set-up, outside the timed region
 
     stream = torch.cuda.current_stream(dev)
     d_pos = torch.from_numpy(pos_host).to(dev)
@@ -271,7 +273,7 @@ def main():
         p_sys = [atm.system_from_case(cases[0])[0]]
         pb = atm.ReplicaBatch(p_sys, local, {"DifferencePath": 0})
         pb.evaluate(cases[0].pos)
-        pb.autotune(trials=5, use_cache=False)
+        pb.autotune(trials=5, use_cache=args.tune_cache)
         dp1 = torch.from_numpy(np.ascontiguousarray(cases[0].pos)).to(dev)
         df1 = torch.empty_like(dp1)
         dr1 = torch.empty((1, atm.NUM_RES), dtype=torch.float64, device=dev)
@@ -280,7 +282,7 @@ def main():
                  "config": "1 replica, two full inner evaluations (reference's path)"}
         pbd = atm.ReplicaBatch([atm.system_from_case(cases[0])[0]], local, {"DifferencePath": 1})
         pbd.evaluate(cases[0].pos)
-        pbd.autotune(trials=5, use_cache=False)
+        pbd.autotune(trials=5, use_cache=args.tune_cache)
         ms_pd = timed_steps(pbd, dp1, df1, dr1, args.steps, args.warmup)
         plain["difference_path_single"] = {"value": 1000.0 / ms_pd, "ms_per_eval": ms_pd}
 

@@ -112,7 +112,11 @@ void launch_prepare(const Args& a, cudaStream_t s) {
 // (the tile finder and the pair-tile kernel live in tiles.cu)
 
 // ---------------------------------------------------------------------------
-// exceptions: FP64, user-order positions; one CTA per 256 exceptions of a replica
+// exceptions: user-order positions; one CTA per 256 exceptions of a replica.
+// Pairs whose two atoms move together have the same separation in both states:
+// their terms are evaluated once, in FP32 (FP64 sums), and enter state 2 with the
+// identical value, so they cancel exactly in u.  Pairs across displacement
+// classes change with the displacement and stay in FP64.
 // ---------------------------------------------------------------------------
 // One exception pair at separation (dx, dy, dz): energy, force on j (f), and
 // (gcorr) erf(alpha r)/r of its Ewald exclusion correction.
@@ -160,6 +164,49 @@ __device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const
     return e;
 }
 
+// FP32 form of exc_term for pairs within one displacement class.
+__device__ __forceinline__ float exc_term_f(const Args& a, const RepDev& R, const ExcParam& p, float dx, float dy,
+                                            float dz, float* f) {
+    float r2 = dx * dx + dy * dy + dz * dz;
+    float e = 0.0f, fr = 0.0f;
+    float px = (float)p.x, pz = (float)p.z;
+    if (px != 0.0f || pz != 0.0f) {
+        float inv_r2 = 1.0f / r2, inv_r = sqrtf(inv_r2);
+        e += px * inv_r;
+        fr += px * inv_r * inv_r2;
+        if (pz != 0.0f) {
+            float py = (float)p.y;
+            float s2 = py * py * inv_r2;
+            float s6 = s2 * s2 * s2;
+            e += 4.0f * pz * (s6 * s6 - s6);
+            fr += 4.0f * pz * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
+        }
+    }
+    f[0] = fr * dx;
+    f[1] = fr * dy;
+    f[2] = fr * dz;
+    if (a.method == 4) {
+        float pw = (float)p.w;
+        float mx = dx - R.box[0] * rintf(dx * R.ibox[0]);
+        float my = dy - R.box[1] * rintf(dy * R.ibox[1]);
+        float mz = dz - R.box[2] * rintf(dz * R.ibox[2]);
+        float m2 = mx * mx + my * my + mz * mz;
+        if (m2 > 0.0f) {
+            float r = sqrtf(m2);
+            float ar = a.alpha * r;
+            float ef = erff(ar);
+            e -= pw * ef / r;
+            float fm = pw * (1.1283791670955126f * a.alpha * expf(-ar * ar) - ef / r) / m2;
+            f[0] += fm * mx;
+            f[1] += fm * my;
+            f[2] += fm * mz;
+        } else {
+            e -= pw * 1.1283791670955126f * a.alpha;
+        }
+    }
+    return e;
+}
+
 __global__ void __launch_bounds__(256) k_exceptions(Args a) {
     __shared__ double red[3][256];
     int c = blockIdx.x;
@@ -174,13 +221,28 @@ __global__ void __launch_bounds__(256) k_exceptions(Args a) {
         const double* di = a.displ_in + 3 * (size_t)ij.x;
         const double* dj = a.displ_in + 3 * (size_t)ij.y;
         int si = a.slot_of[ij.x], sj = a.slot_of[ij.y];
-        double f1[3], f2[3], g1, g2;
-        E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1, &g1);
-        for (int k = 0; k < 3; k++) {
-            fix_add_d(a.F + (size_t)k * a.NA + si, -f1[k]);
-            fix_add_d(a.F + (size_t)k * a.NA + sj, f1[k]);
-        }
-        if (a.full || ij.w) {
+        if (!ij.w) {
+            float g[3];
+            float e1 = exc_term_f(a, R, p, (float)(xj[0] - xi[0]), (float)(xj[1] - xi[1]), (float)(xj[2] - xi[2]), g);
+            E1 = (double)e1;
+            for (int k = 0; k < 3; k++) {
+                fix_add_d(a.F + (size_t)k * a.NA + si, -(double)g[k]);
+                fix_add_d(a.F + (size_t)k * a.NA + sj, (double)g[k]);
+            }
+            if (a.full) {
+                E2 = E1;
+                for (int k = 0; k < 3; k++) {
+                    fix_add_d(a.F + (size_t)(3 + k) * a.NA + si, -(double)g[k]);
+                    fix_add_d(a.F + (size_t)(3 + k) * a.NA + sj, (double)g[k]);
+                }
+            }
+        } else {
+            double f1[3], f2[3], g1, g2;
+            E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1, &g1);
+            for (int k = 0; k < 3; k++) {
+                fix_add_d(a.F + (size_t)k * a.NA + si, -f1[k]);
+                fix_add_d(a.F + (size_t)k * a.NA + sj, f1[k]);
+            }
             E2 = exc_term(a, R, p, (xj[0] + dj[0]) - (xi[0] + di[0]), (xj[1] + dj[1]) - (xi[1] + di[1]),
                           (xj[2] + dj[2]) - (xi[2] + di[2]), f2, &g2);
             if (!a.full) {
