@@ -36,6 +36,7 @@ extern "C" {
 #define ATM_ERR_PARSE 7            /* malformed or unsupported XML (ATMMetaForceProxy.cpp:44) */
 #define ATM_ERR_GROUP 8            /* ATM group among the variable groups (ATMMetaForceImpl.cpp:78-79) */
 #define ATM_ERR_PARTICLES 9        /* particle count/index changed (ReferenceATMMetaForceKernels.cpp:147-154) */
+#define ATM_ERR_CONSTRAINTS 10     /* constraint iterations did not converge (MD driver) */
 
 /* ---- nonbonded methods (OpenMM NonbondedForce::NonbondedMethod numbering) -- */
 #define ATM_NB_NOCUTOFF 0
@@ -157,6 +158,28 @@ int atm_system_set_default_periodic_box_vectors(atm_system_t sys, const double* 
 int atm_system_add_nonbonded(atm_system_t sys, atm_nonbonded_t nb);
 int atm_system_add_atm_force(atm_system_t sys, atm_force_t force);
 
+/* Terms the MD driver integrates alongside the ATM force (the group-0 forces of
+ * python/tests/test_abfe.py:55-103).  They do not enter contexts or batches. */
+/* System::addConstraint: fixed distance (nm); clusters of at most 4 particles /
+ * 6 constraints (rigid water, X-H bonds). */
+int atm_system_add_constraint(atm_system_t sys, int i, int j, double distance, int* index);
+int atm_system_get_num_constraints(atm_system_t sys, int* n);
+/* HarmonicBondForce::addBond: (k/2)(r - length)^2, kJ/mol/nm^2. */
+int atm_system_add_bond(atm_system_t sys, int i, int j, double length, double k);
+/* HarmonicAngleForce::addAngle: (k/2)(theta - angle)^2 at vertex j, radians, kJ/mol/rad^2. */
+int atm_system_add_angle(atm_system_t sys, int i, int j, int l, double angle, double k);
+/* ATMMetaForceUtils.addVsiteRestraintForceCMCM (python/ATMMetaForceUtils.py:79-138):
+ * (kf/2) step(d - tol)(d - tol)^2, d = |c1 - offset - c2|, c the mass-weighted
+ * centroids of g1 (ligand) and g2 (receptor), no periodic image. */
+int atm_system_add_centroid_restraint(atm_system_t sys, int n1, const int* g1, int n2, const int* g2, double kf,
+                                      double tol, const double* offset);
+/* ATMMetaForceUtils.addPosRestraints (python/ATMMetaForceUtils.py:707-752):
+ * 0.5 fc step(d - tol)(d - tol)^2, d the distance to (x0,y0,z0), periodic
+ * (minimum image) unless set_position_restraints_periodic(0). */
+int atm_system_add_position_restraint(atm_system_t sys, int particle, double x0, double y0, double z0, double fc,
+                                      double tol);
+int atm_system_set_position_restraints_periodic(atm_system_t sys, int periodic);
+
 /* ---- Context: one replica on one GPU -------------------------------------- */
 /* properties: "key=value;key=value".  Keys: DifferencePath=0|1 (default 0, two
  * full inner evaluations as in ATMMetaForceImpl.cpp:113,116). */
@@ -215,6 +238,40 @@ int atm_batch_backward_device(atm_batch_t b, const double* d_g, double* d_dx, do
 /* Same with host buffers. */
 int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, double* dq, double* dsig,
                        double* deps, double* dparams);
+
+/* ---- MD: Langevin dynamics of R replicas ------------------------------------ */
+/* OpenMM's LangevinIntegrator (leapfrog: v <- a v + (1-a)/g f/m + sqrt(kT(1-a^2)/m) N,
+ * a = exp(-g dt); x' = x + dt v, constrained; v = (x' - x)/dt) stepping the ATM
+ * force plus each system's bonds, angles and restraints, as the reference's
+ * tests and examples do with integrator.setIntegrationForceGroups({0, ATM group})
+ * (python/tests/test_abfe.py:96-103, example/abfe/abfe.py:94-101).  systems as
+ * for atm_batch_create, plus masses (mass 0: the particle does not move).
+ * properties: DifferencePath=0|1 (default 1), ReorderInterval=steps (default
+ * 0: re-sort when the pair-tile count has grown by 20 %).  temperature K,
+ * friction 1/ps, step_size ps; seed keys the Philox4x32-10 thermostat noise. */
+typedef struct atm_md_s* atm_md_t;
+int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
+                  double temperature, double friction, double step_size, unsigned long long seed, atm_md_t* out);
+int atm_md_destroy(atm_md_t md);
+int atm_md_get_num_particles(atm_md_t md, int* n_total);
+/* Positions / velocities of every replica back to back (host, n_total x 3). */
+int atm_md_set_positions(atm_md_t md, const double* pos);
+int atm_md_set_velocities(atm_md_t md, const double* vel);
+/* Maxwell-Boltzmann velocities at temperature (K) from the seed's Philox stream. */
+int atm_md_set_velocities_to_temperature(atm_md_t md, double temperature, unsigned long long seed);
+int atm_md_set_parameter(atm_md_t md, int replica, const char* name, double value);
+int atm_md_set_integrator(atm_md_t md, double temperature, double friction, double step_size);
+int atm_md_step(atm_md_t md, int steps);
+/* Host outputs, each nullable: positions, velocities (v at t - dt/2), total forces
+ * (n_total x 3); per replica potential energy (bonded + restraints + ATM) and
+ * kinetic energy (velocities shifted by dt/2 f/m, as OpenMM's leapfrog
+ * integrators report it); results (R x ATM_NUM_RES) of the ATM evaluation at
+ * the current positions. */
+int atm_md_get_state(atm_md_t md, double* pos, double* vel, double* forces, double* potential, double* kinetic,
+                     double* results);
+/* Steps taken, re-sorts made, and per replica degrees of freedom
+ * (3 x particles with mass - constraints; dof nullable, R entries). */
+int atm_md_get_info(atm_md_t md, long long* steps, int* reorders, int* dof);
 
 /* ---- allocation-free variant ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc:

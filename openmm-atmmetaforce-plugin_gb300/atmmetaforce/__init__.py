@@ -3,10 +3,15 @@
 Mirrors the reference plugin's Python module ``atmmetaforce``
 (python/atmmetaforceplugin.i): ``ATMMetaForce`` plus the OpenMM stand-ins the
 path needs (``NonbondedForce``, ``System``, ``Context``), a ``ReplicaBatch`` for
-many replicas per launch, and (in ``autograd``) a torch.autograd.Function.
+many replicas per launch, Langevin dynamics of one or many replicas (``md``),
+and (in ``autograd``) a torch.autograd.Function.
 """
+import numpy as np
+
 from ._lib import ATMError, NUM_RES, RES_KEYS
 from .api import ATMMetaForce, Context, NonbondedForce, ReplicaBatch, State, System
+from .md import (ATMMetaForceUtils, HarmonicAngleForce, HarmonicBondForce, LangevinIntegrator, ReplicaSimulation,
+                 Simulation, md_system_from_case)
 
 ATMMETAFORCE_VERSION = "0.3.1"
 
@@ -15,11 +20,12 @@ def system_from_case(case, nonbonded_group=1, atm_group=2, mass=1.0):
     """A System holding the case's NonbondedForce (in ``nonbonded_group``) and an
     ATMMetaForce over every particle (in ``atm_group``, re-evaluating
     ``nonbonded_group``), laid out as the reference's ABFE test builds it
-    (python/tests/test_abfe.py:100-114)."""
+    (python/tests/test_abfe.py:100-114).  ``mass``: one value or one per particle."""
     spec = case.spec
     sys_ = System()
-    for _ in range(case.n):
-        sys_.addParticle(mass)
+    masses = [float(mass)] * case.n if np.isscalar(mass) else [float(m) for m in mass]
+    for m in masses:
+        sys_.addParticle(m)
     L = spec.box
     sys_.setDefaultPeriodicBoxVectors((L[0], 0, 0), (0, L[1], 0), (0, 0, L[2]))
     nb = NonbondedForce()
@@ -47,4 +53,6 @@ def system_from_case(case, nonbonded_group=1, atm_group=2, mass=1.0):
 
 
 __all__ = ["ATMMetaForce", "NonbondedForce", "System", "Context", "State", "ReplicaBatch", "ATMError",
-           "ATMMETAFORCE_VERSION", "system_from_case", "NUM_RES", "RES_KEYS"]
+           "ATMMETAFORCE_VERSION", "system_from_case", "NUM_RES", "RES_KEYS", "HarmonicBondForce",
+           "HarmonicAngleForce", "ATMMetaForceUtils", "LangevinIntegrator", "ReplicaSimulation", "Simulation",
+           "md_system_from_case"]

@@ -19,7 +19,7 @@ RES_KEYS = ("energy", "pert", "sp", "W", "u", "e0", "bfp", "fp", "E1", "E2",
 ATM_ERRORS = {
     1: "invalid argument", 2: "index out of range", 3: "invalid state", 4: "CUDA failure",
     5: "unsupported", 6: "capacity overflow", 7: "XML parse error", 8: "force group conflict",
-    9: "particle set changed",
+    9: "particle set changed", 10: "constraints did not converge",
 }
 
 
@@ -79,6 +79,14 @@ _SIGS = {
     "atm_system_set_default_periodic_box_vectors": [_vp, _dp, _dp, _dp],
     "atm_system_add_nonbonded": [_vp, _vp],
     "atm_system_add_atm_force": [_vp, _vp],
+    "atm_system_add_constraint": [_vp, C.c_int, C.c_int, C.c_double, _ip],
+    "atm_system_get_num_constraints": [_vp, _ip],
+    "atm_system_add_bond": [_vp, C.c_int, C.c_int, C.c_double, C.c_double],
+    "atm_system_add_angle": [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double],
+    "atm_system_add_centroid_restraint": [_vp, C.c_int, _ip, C.c_int, _ip, C.c_double, C.c_double, _dp],
+    "atm_system_add_position_restraint": [_vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_double],
+    "atm_system_set_position_restraints_periodic": [_vp, C.c_int],
     "atm_context_create": [_vp, C.c_int, C.c_char_p, C.POINTER(_vp)],
     "atm_context_destroy": [_vp],
     "atm_context_set_positions": [_vp, _dp, C.c_int],
@@ -106,6 +114,18 @@ _SIGS = {
     "atm_batch_get_kernel_times": [_vp, C.c_char_p, _sz, _dp, C.c_int, _ip],
     "atm_batch_get_launch_count": [_vp, _ip],
     "atm_batch_get_stats": [_vp, _ip, _ip, _ip],
+    "atm_md_create": [C.POINTER(_vp), C.c_int, C.c_int, C.c_char_p, C.c_double, C.c_double, C.c_double,
+                      C.c_ulonglong, C.POINTER(_vp)],
+    "atm_md_destroy": [_vp],
+    "atm_md_get_num_particles": [_vp, _ip],
+    "atm_md_set_positions": [_vp, _dp],
+    "atm_md_set_velocities": [_vp, _dp],
+    "atm_md_set_velocities_to_temperature": [_vp, C.c_double, C.c_ulonglong],
+    "atm_md_set_parameter": [_vp, C.c_int, C.c_char_p, C.c_double],
+    "atm_md_set_integrator": [_vp, C.c_double, C.c_double, C.c_double],
+    "atm_md_step": [_vp, C.c_int],
+    "atm_md_get_state": [_vp, _dp, _dp, _dp, _dp, _dp, _dp],
+    "atm_md_get_info": [_vp, C.POINTER(C.c_longlong), _ip, _ip],
     "atm_rf_nonbonded_noalloc": [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _dp, C.c_double, C.c_double, _vp, _vp,
                                  _vp],
 }

@@ -289,6 +289,7 @@ class System:
         call("atm_system_create", C.byref(h))
         self._h = h
         self._forces = []
+        self._constraints = []
 
     def __del__(self):
         try:
@@ -311,11 +312,28 @@ class System:
         a, b, c = _vec3(a), _vec3(b), _vec3(c)
         call("atm_system_set_default_periodic_box_vectors", self._h, _ptr(a), _ptr(b), _ptr(c))
 
+    def addConstraint(self, particle1, particle2, distance):
+        """System::addConstraint (MD driver only; clusters of at most 4 particles)."""
+        k = C.c_int()
+        call("atm_system_add_constraint", self._h, int(particle1), int(particle2), float(distance), C.byref(k))
+        self._constraints.append((int(particle1), int(particle2), float(distance)))
+        return k.value
+
+    def getNumConstraints(self):
+        n = C.c_int()
+        call("atm_system_get_num_constraints", self._h, C.byref(n))
+        return n.value
+
+    def getConstraintParameters(self, index):
+        return self._constraints[index]
+
     def addForce(self, force):
         if isinstance(force, NonbondedForce):
             call("atm_system_add_nonbonded", self._h, force._h)
         elif isinstance(force, ATMMetaForce):
             call("atm_system_add_atm_force", self._h, force._h)
+        elif hasattr(force, "_attach"):
+            force._attach(self)  # bonded MD terms (atmmetaforce.md)
         else:
             raise ATMError(5, f"unsupported force type {type(force).__name__}")
         force._owned = False  # OpenMM semantics: the System owns its forces

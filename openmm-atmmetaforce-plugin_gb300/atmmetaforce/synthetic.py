@@ -331,3 +331,81 @@ def rbfe_pme_60000(seed=400):
     return water_ligand_box(60000, 8.5, [30, 36], [(2.5, 2.5, 2.5), (-2.5, -2.5, -2.5)], PME, 1.0, seed,
                             params=default_params(0.25, 0.25, 0.1, 110.0, 0.0, 200.0, 100.0, 0.0625, 1.0),
                             name="rbfe-pme-60000")
+
+
+# ---------------------------------------------------------------------------
+# MD terms: the group-0 forces the reference's ABFE test integrates with the
+# ATM force (python/tests/test_abfe.py:55-103)
+# ---------------------------------------------------------------------------
+
+MASS_O, MASS_H, MASS_LIG = 15.999, 1.008, 12.011
+KCAL_A2 = 4.184 * 100.0  # kcal/mol/A^2 in kJ/mol/nm^2
+
+
+@dataclass
+class MDTerms:
+    masses: np.ndarray                  # (n,)
+    constraints: list                   # (i, j, distance)
+    bonds: list                         # (i, j, length, k)
+    angles: list                        # (i, j, l, angle, k)
+    posres_particles: np.ndarray        # restrained "receptor" atoms
+    posres_ref: np.ndarray              # (n, 3) reference positions
+    posres_fc: float
+    posres_tol: float
+    posres_periodic: bool
+    centroid: list                      # (g1, g2, kf, tol, offset)
+
+
+def _angle(a, b, c):
+    u, v = a - b, c - b
+    return math.atan2(np.linalg.norm(np.cross(u, v)), float(np.dot(u, v)))
+
+
+def md_terms(case, n_receptor=8, bond_k=2.5e5, angle_k=500.0, rigid_water=True):
+    """Masses, rigid-water constraints, ligand bonds and angles at their built
+    geometry, and the restraints of the reference's ABFE test: the ``n_receptor``
+    water oxygens nearest the first ligand stand in for the receptor atoms (their
+    molecules moved to the periodic image next to the ligand), held by flat-bottom
+    position restraints (25 kcal/mol/A^2, 0.5 A) and joined to the ligand by a
+    centroid restraint (25 kcal/mol/A^2, 5 A, offset = the starting centroid
+    separation).  Returns (terms, positions)."""
+    pos = case.pos.copy()
+    n = case.n
+    lig_all = np.concatenate(case.ligands) if case.ligands else np.zeros(0, dtype=int)
+    n_water = (n - len(lig_all)) // 3
+    box = case.spec.box
+    masses = np.full(n, MASS_LIG)
+    masses[: 3 * n_water] = np.tile([MASS_O, MASS_H, MASS_H], n_water)
+    cons = []
+    if rigid_water:
+        d_hh = 2.0 * R_OH * math.sin(math.radians(HOH_DEG) / 2.0)
+        for w in range(n_water):
+            o = 3 * w
+            cons += [(o, o + 1, R_OH), (o, o + 2, R_OH), (o + 1, o + 2, d_hh)]
+    bonds, angles = [], []
+    for lig in case.ligands:
+        for a in range(len(lig) - 1):
+            i, j = int(lig[a]), int(lig[a + 1])
+            bonds.append((i, j, float(np.linalg.norm(pos[j] - pos[i])), bond_k))
+        for a in range(len(lig) - 2):
+            i, j, l = int(lig[a]), int(lig[a + 1]), int(lig[a + 2])
+            angles.append((i, j, l, _angle(pos[i], pos[j], pos[l]), angle_k))
+    rec = np.zeros(0, dtype=int)
+    centroid = []
+    if case.ligands and n_water >= n_receptor > 0:
+        lig = case.ligands[0]
+        c_lig = (masses[lig, None] * pos[lig]).sum(0) / masses[lig].sum()
+        O = 3 * np.arange(n_water)
+        d = _min_image(pos[O] - c_lig, box)
+        near = np.argsort((d * d).sum(1), kind="stable")[:n_receptor]
+        for w in near:
+            o = int(O[w])
+            shift = d[w] - (pos[o] - c_lig)  # image of the oxygen next to the ligand
+            pos[o:o + 3] += shift
+        rec = np.sort(O[near])
+        c_rec = (masses[rec, None] * pos[rec]).sum(0) / masses[rec].sum()
+        centroid.append((np.asarray(lig, dtype=int), rec, 25.0 * KCAL_A2, 0.5, c_lig - c_rec))
+    terms = MDTerms(masses=masses, constraints=cons, bonds=bonds, angles=angles, posres_particles=rec,
+                    posres_ref=pos.copy(), posres_fc=25.0 * KCAL_A2, posres_tol=0.05, posres_periodic=True,
+                    centroid=centroid)
+    return terms, pos

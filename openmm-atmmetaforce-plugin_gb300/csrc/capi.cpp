@@ -11,6 +11,7 @@
 
 #include "../../include/atm_capi.h"
 #include "engine.h"
+#include "md.h"
 #include "model.h"
 
 using namespace atm;
@@ -52,6 +53,10 @@ struct atm_batch_s {
     ~atm_batch_s() {
         if (scratch) cudaFree(scratch);
     }
+};
+
+struct atm_md_s {
+    std::unique_ptr<MDDriver> md;
 };
 
 static thread_local std::string g_error;
@@ -479,6 +484,85 @@ int atm_system_add_atm_force(atm_system_t sys, atm_force_t force) {
     API_END
 }
 
+// ---- MD terms of a System --------------------------------------------------
+
+static void check_particle(const System& s, int i) {
+    REQUIRE(i >= 0 && i < (int)s.masses.size(), ATM_ERR_INDEX, "Particle index out of range");
+}
+
+int atm_system_add_constraint(atm_system_t sys, int i, int j, double distance, int* index) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    check_particle(sys->sys, i);
+    check_particle(sys->sys, j);
+    REQUIRE(i != j && distance > 0.0, ATM_ERR_INVALID_ARGUMENT, "Invalid constraint");
+    sys->sys.constraints.push_back({i, j, distance});
+    if (index) *index = (int)sys->sys.constraints.size() - 1;
+    API_END
+}
+
+int atm_system_get_num_constraints(atm_system_t sys, int* n) {
+    API_BEGIN
+    REQUIRE(sys && n, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n = (int)sys->sys.constraints.size();
+    API_END
+}
+
+int atm_system_add_bond(atm_system_t sys, int i, int j, double length, double k) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    check_particle(sys->sys, i);
+    check_particle(sys->sys, j);
+    sys->sys.bonds.push_back({i, j, length, k});
+    API_END
+}
+
+int atm_system_add_angle(atm_system_t sys, int i, int j, int l, double angle, double k) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    check_particle(sys->sys, i);
+    check_particle(sys->sys, j);
+    check_particle(sys->sys, l);
+    sys->sys.angles.push_back({i, j, l, angle, k});
+    API_END
+}
+
+int atm_system_add_centroid_restraint(atm_system_t sys, int n1, const int* g1, int n2, const int* g2, double kf,
+                                      double tol, const double* offset) {
+    API_BEGIN
+    REQUIRE(sys && g1 && g2 && n1 > 0 && n2 > 0, ATM_ERR_INVALID_ARGUMENT, "empty centroid group");
+    CentroidRestraint c;
+    for (int k = 0; k < n1; k++) {
+        check_particle(sys->sys, g1[k]);
+        c.g1.push_back(g1[k]);
+    }
+    for (int k = 0; k < n2; k++) {
+        check_particle(sys->sys, g2[k]);
+        c.g2.push_back(g2[k]);
+    }
+    c.kf = kf;
+    c.tol = tol;
+    for (int k = 0; k < 3; k++) c.offset[k] = offset ? offset[k] : 0.0;
+    sys->sys.centroid_restraints.push_back(c);
+    API_END
+}
+
+int atm_system_add_position_restraint(atm_system_t sys, int particle, double x0, double y0, double z0, double fc,
+                                      double tol) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    check_particle(sys->sys, particle);
+    sys->sys.position_restraints.push_back({particle, x0, y0, z0, fc, tol});
+    API_END
+}
+
+int atm_system_set_position_restraints_periodic(atm_system_t sys, int periodic) {
+    API_BEGIN
+    REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
+    sys->sys.position_restraints_periodic = periodic != 0;
+    API_END
+}
+
 // ---- Context --------------------------------------------------------------
 
 int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out) {
@@ -778,6 +862,112 @@ int atm_batch_get_stats(atm_batch_t b, int* tiles, int* rows, int* max_row) {
     API_BEGIN
     REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
     b->eng->stats(tiles, rows, max_row);
+    API_END
+}
+
+// ---- MD ---------------------------------------------------------------------
+
+int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
+                  double temperature, double friction, double step_size, unsigned long long seed, atm_md_t* out) {
+    API_BEGIN
+    REQUIRE(systems && out && n_replicas > 0, ATM_ERR_INVALID_ARGUMENT, "bad argument");
+    REQUIRE(step_size > 0.0 && friction >= 0.0 && temperature >= 0.0, ATM_ERR_INVALID_ARGUMENT,
+            "Invalid integrator parameters");
+    auto props = parse_props(properties);
+    bool diff = prop_bool(props, "DifferencePath", true);
+    MdOptions opt;
+    opt.temperature = temperature;
+    opt.friction = friction;
+    opt.step_size = step_size;
+    opt.seed = seed;
+    auto it = props.find("ReorderInterval");
+    if (it != props.end()) opt.reorder_interval = std::stoi(it->second);
+    std::vector<const System*> v;
+    for (int r = 0; r < n_replicas; r++) {
+        REQUIRE(systems[r], ATM_ERR_INVALID_ARGUMENT, "null system");
+        v.push_back(&systems[r]->sys);
+    }
+    std::unique_ptr<atm_md_s> m(new atm_md_s);
+    m->md.reset(new MDDriver(v, device, !diff, opt));
+    *out = m.release();
+    API_END
+}
+
+int atm_md_destroy(atm_md_t md) {
+    API_BEGIN
+    delete md;
+    API_END
+}
+
+int atm_md_get_num_particles(atm_md_t md, int* n_total) {
+    API_BEGIN
+    REQUIRE(md && n_total, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    *n_total = md->md->total_atoms();
+    API_END
+}
+
+int atm_md_set_positions(atm_md_t md, const double* pos) {
+    API_BEGIN
+    REQUIRE(md && pos, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->set_positions(pos);
+    API_END
+}
+
+int atm_md_set_velocities(atm_md_t md, const double* vel) {
+    API_BEGIN
+    REQUIRE(md && vel, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->set_velocities(vel);
+    API_END
+}
+
+int atm_md_set_velocities_to_temperature(atm_md_t md, double temperature, unsigned long long seed) {
+    API_BEGIN
+    REQUIRE(md && temperature >= 0.0, ATM_ERR_INVALID_ARGUMENT, "bad argument");
+    md->md->set_velocities_to_temperature(temperature, seed);
+    API_END
+}
+
+int atm_md_set_parameter(atm_md_t md, int replica, const char* name, double value) {
+    API_BEGIN
+    REQUIRE(md && name, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    REQUIRE(replica >= 0 && replica < md->md->replicas(), ATM_ERR_INDEX, "Replica index out of range");
+    int w = global_index(name);
+    REQUIRE(w >= 0, ATM_ERR_INVALID_ARGUMENT, std::string("Unknown parameter: ") + name);
+    md->md->set_param(replica, w, value);
+    API_END
+}
+
+int atm_md_set_integrator(atm_md_t md, double temperature, double friction, double step_size) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->set_integrator(temperature, friction, step_size);
+    API_END
+}
+
+int atm_md_step(atm_md_t md, int steps) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->step(steps);
+    API_END
+}
+
+int atm_md_get_state(atm_md_t md, double* pos, double* vel, double* forces, double* potential, double* kinetic,
+                     double* results) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->get_state(pos, vel, forces, potential, kinetic, results);
+    API_END
+}
+
+int atm_md_get_info(atm_md_t md, long long* steps, int* reorders, int* dof) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    if (steps) *steps = md->md->step_count();
+    if (reorders) *reorders = md->md->reorders();
+    if (dof) {
+        const auto& d = md->md->degrees_of_freedom();
+        for (size_t r = 0; r < d.size(); r++) dof[r] = d[r];
+    }
     API_END
 }
 

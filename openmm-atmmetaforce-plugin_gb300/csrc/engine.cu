@@ -1067,7 +1067,7 @@ void Engine::evaluate(double* energies, double* forces, double* forces_nb, doubl
     if (matrix) std::memcpy(matrix, h_matrix_, sizeof(double) * (size_t)R_ * R_);
 }
 
-void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream) {
+void Engine::run_device(const double* d_pos, cudaStream_t stream) {
     CUDA_CHECK(cudaSetDevice(dev_));
     if (!layout_ready_) {
         // the layout is built from positions: take them to the host once
@@ -1077,6 +1077,17 @@ void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_re
         alloc_device();
     }
     run(false, stream, d_pos);
+}
+
+void Engine::reorder_from_device(const double* d_pos, cudaStream_t stream) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    CUDA_CHECK(cudaMemcpyAsync(h_pos_, d_pos, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost, stream));
+    CUDA_CHECK(cudaStreamSynchronize(stream));
+    layout_ready_ = false;
+}
+
+void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream) {
+    run_device(d_pos, stream);
     if (d_forces)
         CUDA_CHECK(cudaMemcpyAsync(d_forces, A_.f_out, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToDevice,
                                    stream));

@@ -63,6 +63,15 @@ public:
     void evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix);
     // Device path on the caller's stream.
     void evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream);
+    // Device path without output copies: after it returns, forces_device() and
+    // results_device() hold the evaluation at d_pos (valid until the next call).
+    void run_device(const double* d_pos, cudaStream_t stream);
+    const double* forces_device() const { return A_.f_out; }
+    const double* results_device() const { return A_.results; }
+    const double* box(int r) const { return specs_[r].box; }
+    // Re-sort from device positions at the next evaluation (the layout, tile
+    // rows and exclusion masks are rebuilt; results do not change).
+    void reorder_from_device(const double* d_pos, cudaStream_t stream);
 
     // Re-sort atoms from the current positions (exclusion masks follow).
     void reorder();

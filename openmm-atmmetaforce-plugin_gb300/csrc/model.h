@@ -72,6 +72,35 @@ public:
     int forceGroup = 0;
 };
 
+// Terms integrated alongside the ATM force by the MD driver (force group 0 of
+// the reference's test and examples: python/tests/test_abfe.py:101-103).
+struct Bond {  // OpenMM HarmonicBondForce: (k/2)(r - length)^2, no periodic image
+    int i, j;
+    double length, k;
+};
+struct Angle {  // OpenMM HarmonicAngleForce: (k/2)(theta - angle)^2 at vertex j
+    int i, j, l;
+    double angle, k;
+};
+struct Constraint {  // System::addConstraint: fixed distance between two particles
+    int i, j;
+    double distance;
+};
+// Flat-bottom harmonic restraint between the mass-weighted centroids of two
+// particle groups: (kf/2) step(d - tol) (d - tol)^2, d = |c1 - offset - c2|, no
+// periodic image (python/ATMMetaForceUtils.py:79-138, addVsiteRestraintForceCMCM).
+struct CentroidRestraint {
+    std::vector<int> g1, g2;
+    double kf, tol;
+    double offset[3];
+};
+// Flat-bottom harmonic position restraint: 0.5 fc step(d - tol)(d - tol)^2 with
+// d the (periodic) distance to (x0, y0, z0) (python/ATMMetaForceUtils.py:707-752).
+struct PositionRestraint {
+    int particle;
+    double x0, y0, z0, fc, tol;
+};
+
 class System {
 public:
     int addParticle(double m) {
@@ -82,6 +111,12 @@ public:
     double box[3] = {2.0, 2.0, 2.0};  // OpenMM's default box
     std::unique_ptr<NonbondedForce> nonbonded;
     std::unique_ptr<ATMMetaForce> atm;
+    std::vector<Bond> bonds;
+    std::vector<Angle> angles;
+    std::vector<Constraint> constraints;
+    std::vector<CentroidRestraint> centroid_restraints;
+    std::vector<PositionRestraint> position_restraints;
+    bool position_restraints_periodic = true;
 };
 
 // XML of serialization/src/ATMMetaForceProxy.cpp:11-79 inside OpenMM's
