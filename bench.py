@@ -28,17 +28,22 @@ sys.path.insert(0, os.path.join(ROOT, "openmm-atmmetaforce-plugin_gb300"))
 METRIC = "ATM evals/sec/replica at 23.5k-atom PME: batched vs plain on one GB300 at fixed error"
 F_PAIR = 55.0  # FP32 flops per pair (accounting constant)
 L2_BYTES = 129 * 1024 * 1024
+# DRAM bytes (read + write) of one k_tiles launch on this workload, from an ncu
+# --set full capture (78.50 MB read + 2.85 MB write)
+TILES_TRAFFIC_BYTES = 81.34e6
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--replicas", type=int, default=22)
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-md", action="store_true", help="skip the MD step-rate measurements")
+    p.add_argument("--md-steps", type=int, default=200)
     p.add_argument("--tune-cache", action="store_true",
                    help="reuse a stored autotuning choice for this GPU and workload (profiling runs)")
     return p.parse_args()
@@ -88,10 +93,14 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0:  # sampling has started before the timed region
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -197,6 +206,42 @@ def reference_arm(args, rank, world, pg):
                              "sample": f"{args.steps} evaluations of one 23,558-atom replica"},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def md_bench(cases_fn, R, steps, warmup, device):
+    """Langevin MD step rate of R replicas stepped together (OpenMM's
+    LangevinIntegrator settings of the reference's ABFE test: 300 K, 0.5/ps,
+    1 fs; rigid water).  Host wall clock around ``step(steps)``, which ends with a
+    device synchronisation; every step is one batched ATM evaluation plus the
+    group-0 terms, the Langevin update, SETTLE and the velocity update."""
+    import atmmetaforce as atm
+    from atmmetaforce import synthetic as S
+
+    cases, terms = [], []
+    for r in range(R):
+        c = cases_fn(r)
+        t, p = S.md_terms(c)
+        c.pos = p
+        cases.append(c)
+        terms.append(t)
+    systems = [atm.md_system_from_case(c, t)[0] for c, t in zip(cases, terms)]
+    dt = 0.001
+    integ = atm.LangevinIntegrator(300.0, 0.5, dt)
+    integ.setRandomNumberSeed(2024)
+    sim = atm.ReplicaSimulation(systems, integ, device)
+    sim.setPositions(np.concatenate([c.pos for c in cases]))
+    sim.setVelocitiesToTemperature(300.0, 7)
+    sim.step(warmup)
+    t0 = time.perf_counter()
+    sim.step(steps)
+    el = time.perf_counter() - t0
+    sps = steps / el
+    n_atoms = int(sum(c.n for c in cases))
+    out = {"replicas": R, "atoms": n_atoms, "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 * el / steps,
+           "steps_per_s": sps, "step_size_ps": dt, "ns_per_day_per_replica": sps * dt * 86400.0 / 1000.0,
+           "ns_per_day_aggregate": R * sps * dt * 86400.0 / 1000.0, "reorders": sim.info()["reorders"]}
+    del sim
+    return out
 
 
 def main():
@@ -313,12 +358,32 @@ def main():
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops / t_tiles / 1e12
     roofline = {"bound": "fp32", "kernel": "k_tiles (pair tiles)", "achieved": achieved, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": TILES_TRAFFIC_BYTES,
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_tiles launch, ncu --set full "
+                                  "capture of this workload (bytes per launch)",
                 "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
                 "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt, "tile_stats": batch.stats(),
                 "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 1024 * batch.stats()["tiles"])}
+
+    md = None
+    if not args.no_md:
+        from atmmetaforce import synthetic as S
+
+        def abfe(r):
+            l1, l2 = S.SCHEDULE_22[r % 22]
+            return S.abfe_pme_23558(seed=100 + 1000 * rank + r, lambdas=(l1, l2), alpha=0.1, u0=110.0)
+
+        def rbfe(r):
+            l1, l2 = S.SCHEDULE_22[r % 22]
+            c = S.rbfe_pme_60000(seed=400 + 1000 * rank + r)
+            c.params = S.default_params(l1, l2, 0.1, 110.0, 0.0, 200.0, 100.0, 0.0625, 1.0)
+            return c
+
+        md = {"abfe-pme-23558 x1": md_bench(abfe, 1, 5 * args.md_steps, 20, local),
+              "abfe-pme-23558 x22": md_bench(abfe, 22, args.md_steps, 20, local),
+              "rbfe-pme-60000 x22": md_bench(rbfe, 22, max(20, args.md_steps // 2), 10, local)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -344,7 +409,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": batch.launchCount() * args.steps,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary()}
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "md": md}
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
