@@ -460,17 +460,25 @@ class ReplicaBatch:
         a, b, c = _vec3(a), _vec3(b), _vec3(c)
         call("atm_batch_set_periodic_box_vectors", self._h, int(replica), _ptr(a), _ptr(b), _ptr(c))
 
-    def evaluate(self, positions=None, forces=True):
+    def evaluate(self, positions=None, forces=True, out=None):
         """Evaluate every replica.  positions: None (stored) or an array of
         shape (sum n, 3).  Returns (energies[R], forces[(sum n), 3] or None,
-        results: list of dicts)."""
+        results: list of dicts).  ``out``: a C-contiguous float64 (sum n, 3)
+        array to receive the forces.  Page-locked buffers (e.g. from
+        ``torch.empty(..., pin_memory=True).numpy()``) are copied to and from the
+        GPU directly, without a staging copy."""
         pos = None
         if positions is not None:
             pos = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).reshape(-1, 3))
             if len(pos) != self.offsets[-1]:
                 raise ATMError(1, "wrong number of positions")
         E = np.zeros(self.R)
-        F = np.zeros((self.offsets[-1], 3)) if forces else None
+        if out is not None:
+            if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != 3 * self.offsets[-1]:
+                raise ATMError(1, "out must be a C-contiguous float64 array of (sum n) x 3")
+            F = out
+        else:
+            F = np.zeros((self.offsets[-1], 3)) if forces else None
         res = np.zeros((self.R, NUM_RES))
         call("atm_batch_evaluate", self._h, _ptr(pos) if pos is not None else None, _ptr(E),
              _ptr(F) if F is not None else None, _ptr(res))

@@ -78,7 +78,7 @@ def build(force=False, verbose=False):
     libdir = _cuda_lib_dir()
     tmp = LIB + ".tmp"
     cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + \
-        ["-L" + libdir, "-lcufft", "-Xlinker", "-rpath=" + libdir]
+        ["-L" + libdir, "-lcufft", "-lpthread", "-Xlinker", "-rpath=" + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -733,8 +733,7 @@ int atm_batch_set_periodic_box_vectors(atm_batch_t b, int replica, const double*
 int atm_batch_evaluate(atm_batch_t b, const double* pos_all, double* energies, double* forces, double* results) {
     API_BEGIN
     REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
-    if (pos_all) b->eng->set_all_positions(pos_all);
-    b->eng->evaluate(energies, forces, nullptr, b->results.data(), b->matrix.data());
+    b->eng->evaluate_host(pos_all, energies, forces, nullptr, b->results.data(), b->matrix.data());
     if (results) std::memcpy(results, b->results.data(), sizeof(double) * b->results.size());
     b->evaluated = true;
     API_END

@@ -18,6 +18,7 @@
 #include <map>
 #include <numeric>
 #include <set>
+#include <thread>
 #include <sstream>
 #include <unordered_set>
 
@@ -948,7 +949,7 @@ bool Engine::check_status_and_grow() {
     return true;
 }
 
-void Engine::run(bool host_io, cudaStream_t user, const double* d_pos) {
+void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned) {
     CUDA_CHECK(cudaSetDevice(dev_));
     if (!layout_ready_) {
         build_layout();
@@ -960,6 +961,9 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos) {
         if (d_pos)
             CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
                                        cudaMemcpyDeviceToDevice, st));
+        if (h_pos_pinned)
+            CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, h_pos_pinned, sizeof(double) * 3 * (size_t)n_in_,
+                                       cudaMemcpyHostToDevice, st));
         if (profiling_) {
             // eager launches bracketed by events, one stream, for per-kernel timings
             times_.clear();
@@ -1056,13 +1060,70 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos) {
     throw Error(6, "Tile list capacity could not be established");
 }
 
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister) can be the source or
+// target of an asynchronous copy without a staging copy.
+static bool is_pinned(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// Host copy split over a few threads (a single core moves ~10-20 GB/s).
+static void par_memcpy(void* dst, const void* src, size_t bytes) {
+    const size_t kMin = size_t(4) << 20;
+    int nt = (int)std::min<size_t>(8, std::max<size_t>(1, bytes / kMin));
+    if (nt <= 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    std::vector<std::thread> th;
+    size_t chunk = (bytes + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        size_t b = (size_t)t * chunk, e = std::min(bytes, b + chunk);
+        if (b < e) th.emplace_back([=] { std::memcpy((char*)dst + b, (const char*)src + b, e - b); });
+    }
+    for (auto& x : th) x.join();
+}
+
 void Engine::evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix) {
-    run(true, nullptr, nullptr);
+    evaluate_host(nullptr, energies, forces, forces_nb, results, matrix);
+}
+
+void Engine::evaluate_host(const double* pos, double* energies, double* forces, double* forces_nb, double* results,
+                           double* matrix) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    const size_t bytes = sizeof(double) * 3 * (size_t)n_in_;
+    const bool pin_in = pos && is_pinned(pos);
+    // the layout and the profiling path read the staging copy
+    if (pos && (!pin_in || !layout_ready_ || profiling_)) par_memcpy(h_pos_, pos, bytes);
+    if (profiling_) {
+        run(true, nullptr, nullptr);
+    } else {
+        // positions straight from a pinned caller buffer, else from the pinned staging copy
+        run(false, s_main_, nullptr, pin_in ? pos : h_pos_);
+        const bool pin_out = forces && is_pinned(forces);
+        cudaStream_t st = s_main_;
+        CUDA_CHECK(cudaMemcpyAsync(h_results_, A_.results, sizeof(double) * NUM_RES * (size_t)R_,
+                                   cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(h_matrix_, A_.matrix, sizeof(double) * (size_t)R_ * R_, cudaMemcpyDeviceToHost,
+                                   st));
+        if (forces)
+            CUDA_CHECK(cudaMemcpyAsync(pin_out ? forces : h_forces_, A_.f_out, bytes, cudaMemcpyDeviceToHost, st));
+        if (forces_nb) CUDA_CHECK(cudaMemcpyAsync(h_fnb_, A_.f_nb, bytes, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (forces && !pin_out) par_memcpy(forces, h_forces_, bytes);
+        if (forces_nb) par_memcpy(forces_nb, h_fnb_, bytes);
+        forces = nullptr;
+        forces_nb = nullptr;
+    }
     for (int r = 0; r < R_; r++) {
         if (energies) energies[r] = h_results_[(size_t)r * NUM_RES + RES_ENERGY];
     }
-    if (forces) std::memcpy(forces, h_forces_, sizeof(double) * 3 * (size_t)n_in_);
-    if (forces_nb) std::memcpy(forces_nb, h_fnb_, sizeof(double) * 3 * (size_t)n_in_);
+    if (forces) std::memcpy(forces, h_forces_, bytes);
+    if (forces_nb) std::memcpy(forces_nb, h_fnb_, bytes);
     if (results) std::memcpy(results, h_results_, sizeof(double) * NUM_RES * (size_t)R_);
     if (matrix) std::memcpy(matrix, h_matrix_, sizeof(double) * (size_t)R_ * R_);
 }

@@ -61,6 +61,10 @@ public:
 
     // Host path: positions from the staging copy; outputs to host (nullable).
     void evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix);
+    // Host path with the caller's positions (nullable: the staging copy).  Page-locked
+    // caller buffers are copied from / to directly; others go through pinned staging.
+    void evaluate_host(const double* pos, double* energies, double* forces, double* forces_nb, double* results,
+                       double* matrix);
     // Device path on the caller's stream.
     void evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream);
     // Device path without output copies: after it returns, forces_device() and
@@ -111,7 +115,7 @@ private:
     void fill_args();
     void update_rep_table();
     void record(cudaStream_t main, bool host_io);
-    void run(bool host_io, cudaStream_t user, const double* d_pos);
+    void run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned = nullptr);
     bool check_status_and_grow();
     void destroy_graphs();
 
