@@ -7,8 +7,9 @@
 //     exclusion, with a 32 x 32 exclusion mask;
 //   - atom tiles: the atoms j of every other candidate block J (bounding boxes
 //     closer than the cutoff) that lie within the cutoff of block I's bounding
-//     box, packed 32 per tile.
-// The per-atom test removes most of the pair slots a 32 x 32 block tile would
+//     box and then within the cutoff of at least one atom of block I, packed 32
+//     per tile.
+// The per-atom tests remove most of the pair slots a 32 x 32 block tile would
 // spend beyond the cutoff.
 //
 // Tile entry (int4):
@@ -67,13 +68,18 @@ __device__ __forceinline__ void row_box(const Args& a, int I, int kind, float4& 
 // One pass over the candidate blocks of a row (bounding boxes closer than the
 // cutoff, no exclusion with I) and their atoms within the cutoff of block I's
 // box.  Counts the atoms; with out != nullptr also writes the first cap of them,
-// in a fixed order, to consecutive j slots.
+// in a fixed order, to consecutive j slots.  The row's exclusion partners are
+// held one per lane (rows with more than 32 fall back to reading the list), and
+// four candidate blocks are loaded per step so that their latencies overlap.
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
                                          const int2* ee, int e0, int e1, int lane, int* out, int cap) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
     const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
+    const float4* BH = kind == ROW_STATE2 ? a.bb_h2 : a.bb_h;
+    const int nex = e1 - e0;
+    const int my_ex = lane < nex ? ee[e0 + lane].x : -1;
     int natom = 0;
     const int jb = diff ? R.block_begin : I + 1;
     for (int base = jb; base < R.block_end; base += 32) {
@@ -99,41 +105,51 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
                 }
             }
             ok = boxes_close(ci, hi, cj4, hj4, R, a.rc2);
-            for (int k = e0; ok && k < e1; k++)
-                if (ee[k].x == Jl) ok = false;
+            if (nex > 32)
+                for (int k = e0; ok && k < e1; k++)
+                    if (ee[k].x == Jl) ok = false;
+        }
+        if (nex <= 32) {
+            // drop the exclusion partners: lane q holds partner q
+            for (int q = 0; q < nex; q++) {
+                const int xj = __shfl_sync(FULL_MASK, my_ex, q);
+                if (xj == Jl) ok = false;
+            }
         }
         unsigned cand = __ballot_sync(FULL_MASK, ok);
-        // two candidate blocks per step so that their loads overlap
         while (cand) {
-            const int J1 = base + __ffs(cand) - 1;
-            cand &= cand - 1;
-            const int J2 = cand ? base + __ffs(cand) - 1 : -1;
-            if (cand) cand &= cand - 1;
-            const int j1 = J1 * kTile + lane;
-            const int j2 = (J2 >= 0 ? J2 : J1) * kTile + lane;
-            float4 p1 = P[j1], p2 = P[j2];
-            const int n1 = __float_as_int((kind == ROW_STATE2 ? a.bb_h2 : a.bb_h)[J1].w);
-            const int n2 = J2 >= 0 ? __float_as_int((kind == ROW_STATE2 ? a.bb_h2 : a.bb_h)[J2].w) : 0;
+            int J[4], n[4];
+            float4 p[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                J[t] = cand ? base + __ffs(cand) - 1 : -1;
+                if (cand) cand &= cand - 1;
+            }
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int jj = (J[t] >= 0 ? J[t] : J[0]) * kTile + lane;
+                p[t] = P[jj];
+                n[t] = J[t] >= 0 ? __float_as_int(BH[J[t]].w) : 0;
+            }
             if (g2) {
-                const float4 d1 = a.displ[j1], d2 = a.displ[j2];
-                p1.x += d1.x;
-                p1.y += d1.y;
-                p1.z += d1.z;
-                p2.x += d2.x;
-                p2.y += d2.y;
-                p2.z += d2.z;
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const float4 d = a.displ[(J[t] >= 0 ? J[t] : J[0]) * kTile + lane];
+                    p[t].x += d.x;
+                    p[t].y += d.y;
+                    p[t].z += d.z;
+                }
             }
-            const bool in1 = lane < n1 && point_close(ci, hi, p1, R, a.rc2);
-            const bool in2 = lane < n2 && point_close(ci, hi, p2, R, a.rc2);
-            const unsigned b1 = __ballot_sync(FULL_MASK, in1);
-            const unsigned b2 = __ballot_sync(FULL_MASK, in2);
-            if (out) {
-                const unsigned lt = (1u << lane) - 1u;
-                const int k1 = natom + __popc(b1 & lt), k2 = natom + __popc(b1) + __popc(b2 & lt);
-                if (in1 && k1 < cap) out[k1] = j1;
-                if (in2 && k2 < cap) out[k2] = j2;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const bool in = lane < n[t] && point_close(ci, hi, p[t], R, a.rc2);
+                const unsigned b = __ballot_sync(FULL_MASK, in);
+                if (out) {
+                    const int k = natom + __popc(b & ((1u << lane) - 1u));
+                    if (in && k < cap) out[k] = J[t] * kTile + lane;
+                }
+                natom += __popc(b);
             }
-            natom += __popc(b1) + __popc(b2);
         }
     }
     return natom;
@@ -141,11 +157,68 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
 
 constexpr int kStageAtoms = 1024;  // culled atoms staged in shared memory per row
 
+// Position of slot s at the geometry of a row kind, as the pair-tile kernel reads it.
+__device__ __forceinline__ float4 row_pos(const Args& a, int kind, int s) {
+    float4 p = (kind == ROW_STATE2 ? a.posq2 : a.posq)[s];
+    if (kind == ROW_DIFF2) {
+        const float4 d = a.displ[s];
+        p.x += d.x;
+        p.y += d.y;
+        p.z += d.z;
+    }
+    return p;
+}
+
+// Second cut of a staged row: keeps the atoms j within the cutoff of at least one
+// atom of block I (the box test keeps every atom within the cutoff of the box,
+// corners included).  Positions are taken to the periodic image nearest the
+// box centre, as the pair-tile kernel does; the threshold is widened by 1e-5 so
+// that no pair the kernel counts can be dropped by rounding.  In place, order kept.
+__device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int I, int kind, float4 ci, int lane,
+                                         int* list, int natom, float4* s_ipos) {
+    float4 pi = row_pos(a, kind, I * kTile + lane);
+    pi.x = ci.x + min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
+    pi.y = ci.y + min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
+    pi.z = ci.z + min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
+    s_ipos[lane] = pi;
+    __syncwarp();
+    const float rc2 = a.rc2 * 1.00001f;
+    int kept = 0;
+    for (int g = 0; g < natom; g += 32) {
+        const int k = g + lane;
+        const bool valid = k < natom;
+        const int j = valid ? list[k] : 0;
+        bool hit = false;
+        if (valid) {
+            float4 p = row_pos(a, kind, j);
+            p.x = ci.x + min_img(p.x - ci.x, R.box[0], R.ibox[0]);
+            p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
+            p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
+#pragma unroll 8
+            for (int q = 0; q < 32; q++) {
+                const float4 o = s_ipos[q];
+                const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
+                hit |= dx * dx + dy * dy + dz * dz < rc2;
+            }
+        }
+        __syncwarp();
+        const bool keep = valid && hit;
+        const unsigned b = __ballot_sync(FULL_MASK, keep);
+        if (keep) list[kept + __popc(b & ((1u << lane) - 1u))] = j;
+        kept += __popc(b);
+        __syncwarp();
+    }
+    return kept;
+}
+
 __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     __shared__ int s_stage[kFindWarps][kStageAtoms];
+    __shared__ float4 s_ipos[kFindWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int row = blockIdx.x * kFindWarps + w;
-    if (row >= a.nrows) return;
+    // last rows first: the state-2 / difference rows at the end of the row list
+    // scan every block of their replica and are the longest, so they start early
+    const int row = a.nrows - 1 - (blockIdx.x * kFindWarps + w);
+    if (row < 0) return;
     const int4 d = a.row_desc[row];
     const int I = d.x, kind = d.y;
     const RepDev& R = a.reps[d.z];
@@ -155,9 +228,17 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     const int e0 = es[I], e1 = es[I + 1];
     float4 ci, hi;
     row_box(a, I, kind, ci, hi);
+    // pbc: some pair of an atom tile may need its own minimum image when the
+    // cutoff sphere around block I reaches half a box length
+    const float rc = sqrtf(a.rc2);
+    const unsigned pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
+                          rc + 2.f * hi.z >= 0.5f * R.box[2])
+                             ? 1u
+                             : 0u;
     // staged in shared memory; rows longer than the stage are written by a second pass
-    const int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, s_stage[w], kStageAtoms);
+    int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, s_stage[w], kStageAtoms);
     __syncwarp();
+    if (natom <= kStageAtoms && !pbc) natom = exact_cut(a, R, I, kind, ci, lane, s_stage[w], natom, s_ipos[w]);
     const int nblock = e1 - e0;
     const int natile = (natom + 31) / 32;
     int n = nblock + natile;
@@ -183,13 +264,6 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
         row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom);
     }
     for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
-    // pbc: some pair of an atom tile may need its own minimum image when the
-    // cutoff sphere around block I reaches half a box length
-    const float rc = sqrtf(a.rc2);
-    const unsigned pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
-                          rc + 2.f * hi.z >= 0.5f * R.box[2])
-                             ? 1u
-                             : 0u;
     const int zword = row | (kind << 28);
     for (int k = lane; k < nblock; k += 32) {
         const int2 e = ee[e0 + k];
