@@ -609,7 +609,8 @@ void Engine::build_bricks() {
         rd.brick_cta_b = (int)brick_cta_rep_.size();
         int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
         for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
-        brick_smem_ = std::max(brick_smem_, (int)(sizeof(unsigned long long) * rd.bsz[0] * rd.bsz[1] * rd.bsz[2]));
+        // int32 accumulator of a brick padded by the stencil reach (4 points) on each side
+        brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + 8) * (rd.bsz[1] + 8) * (rd.bsz[2] + 8)));
     }
 }
 

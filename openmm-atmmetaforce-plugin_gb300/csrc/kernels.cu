@@ -328,14 +328,22 @@ __device__ __forceinline__ void make_stencil(float x, float y, float z, const Re
 }
 
 // Charge spreading by bricks.  One CTA owns one brick (at most 16^3 points) of
-// one of a replica's two charge grids.  It finds the 32-atom blocks whose
-// stencils can reach the brick (bounding boxes in grid units, one point of
-// margin for rounding), accumulates their contributions as int64 fixed point
-// in shared memory (exact and order independent), and writes every point of
-// its brick once as a float.  Grid 0: state 1.  Grid 1: state 2 (two-state mode)
-// or the structure-factor update of the moving atoms, -q at x and +q at x + d
-// (difference mode).
+// one of a replica's two charge grids.  It lists the atoms whose 5x5x5 stencils
+// reach the brick (block bounding boxes in grid units first, one point of
+// margin for rounding) and adds every stencil into an int32 fixed-point copy of
+// the brick padded by 4 points on each side (2^25 units per e: integer sums are
+// exact and order independent, so the grid is bit-reproducible), one atom per
+// warp at a time with the lanes on its 5x5 (y, z) offsets.  With the padding no
+// stencil point needs a bounds test; the padding belongs to the neighbouring
+// bricks, which add the same atoms themselves, and only the brick's own points
+// are written, each once.  Grids smaller than a padded brick use the same copy
+// unpadded, with per-point tests.  Grid 0: state 1.  Grid 1: state 2 (two-state
+// mode) or the structure-factor update of the moving atoms, -q at x and +q at
+// x + d (difference mode).
 constexpr int kBrickThreads = 256;
+constexpr int kBrickWarps = kBrickThreads / 32;
+constexpr int kBrickPad = kOrder - 1;      // stencil reach below and above a brick
+constexpr float kGridScale = 33554432.0f;  // 2^25 fixed-point units per e
 
 // Does the cyclic range of base indices of a box (centre c, half extent h, nm)
 // meet the cyclic interval [o, o + len) of Z_K?
@@ -359,30 +367,11 @@ __device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev
 }
 
 constexpr int kSpreadChunk = kBrickThreads;  // blocks examined per pass (one per thread)
-constexpr int kSpreadBatch = 16;             // candidate blocks whose atoms are listed at once
-constexpr int kSpreadList = kSpreadBatch * kTile;
-constexpr int kStencilFloats = 3 * kOrder;   // q*wx, wy, wz of one listed atom
+constexpr int kStencilWords = 16;            // q*wx[5], wy[5], wz[5], packed bases
 
-// Dynamic shared memory of a spreading CTA: accumulators plus listed stencils.
-int spread_smem_bytes(int accum_bytes) { return accum_bytes + kSpreadList * kStencilFloats * (int)sizeof(float); }
-
-__device__ __forceinline__ float pick5(const float* w, int k) {
-    return k == 0 ? w[0] : k == 1 ? w[1] : k == 2 ? w[2] : k == 3 ? w[3] : w[4];
-}
-
-// Position and signed charge of a spreading entry (code: 0 state 1 +q, 1 state 1
-// -q, 2 state 2 +q, 3 state 1 displaced +q).
-__device__ __forceinline__ float4 entry_atom(const Args& a, const RepDev& R, int s, int code) {
-    float4 p = code == 2 ? a.posq2[s] : a.posq[s];
-    if (code == 1) p.w = -p.w;
-    if (code == 3) {
-        const float4 dd = a.displ[s];
-        p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
-        p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
-        p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
-    }
-    return p;
-}
+// Dynamic shared memory of a spreading CTA: the brick accumulator (accum_bytes)
+// plus each warp's 32 staged stencils.
+int spread_smem_bytes(int accum_bytes) { return accum_bytes + kBrickWarps * 32 * kStencilWords * (int)sizeof(float); }
 
 // Local index of grid point base - k in a brick [o, o + e), or -1.
 __device__ __forceinline__ int brick_local(int base, int k, int o, int e, int K) {
@@ -393,12 +382,9 @@ __device__ __forceinline__ int brick_local(int base, int k, int o, int e, int K)
 }
 
 __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
-    // int64 fixed-point sums kept exactly as two 32-bit words: hi (value >> 16,
-    // signed) and lo (value & 0xffff), so that native 32-bit shared atomics suffice
-    extern __shared__ int s_acc[];
+    extern __shared__ int s_dyn[];
     __shared__ int s_cand[2 * kSpreadChunk];
-    __shared__ int s_list[kSpreadList];
-    __shared__ int s_ncand, s_nlist;
+    __shared__ int s_wcount[kBrickWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c = blockIdx.x;
     const RepDev& R = a.reps[a.brick_cta_rep[c]];
@@ -413,112 +399,153 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
         e[d] = min(R.bsz[d], R.K[d] - o[d]);
     }
     const int npts = e[0] * e[1] * e[2];
-    const int cap_pts = a.brick_smem / 8;
-    int* s_hi = s_acc;
-    unsigned* s_lo = (unsigned*)(s_acc + cap_pts);
-    float* s_w = (float*)(s_acc + 2 * cap_pts);
-    for (int k = tid; k < npts; k += kBrickThreads) {
-        s_hi[k] = 0;
-        s_lo[k] = 0u;
+    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    float* G = a.qreal + R.real_off + (size_t)g * G3;
+    // the structure-factor update has only the moving blocks (the last blocks of
+    // the replica); a brick none of them reaches is written as zeros
+    const bool upd = g == 1 && !a.full;
+    const int jbegin = upd ? R.mov_block_begin : R.block_begin;
+    if (upd) {
+        bool any = false;
+        for (int J = jbegin + tid; J < R.block_end; J += kBrickThreads) {
+            const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
+            const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
+            any = any || box_meets_brick(c1, h1, R, o, e) || box_meets_brick(c2, h1, R, o, e);
+        }
+        if (!__syncthreads_or(any)) {
+            for (int k = tid; k < npts; k += kBrickThreads) {
+                const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
+                G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = 0.0f;
+            }
+            return;
+        }
     }
-    for (int base = R.block_begin; base < R.block_end; base += kSpreadChunk) {
-        if (tid == 0) s_ncand = 0;
-        __syncthreads();
-        // 1. blocks whose bounding box reaches the brick
+    // padded copy when the grid is larger than a padded brick in every dimension
+    const bool padded = R.K[0] >= e[0] + 2 * kBrickPad && R.K[1] >= e[1] + 2 * kBrickPad &&
+                        R.K[2] >= e[2] + 2 * kBrickPad;
+    const int pad = padded ? kBrickPad : 0;
+    const int P0 = e[0] + 2 * pad, P1 = e[1] + 2 * pad, P2 = e[2] + 2 * pad;
+    int* acc = s_dyn;
+    float* st = (float*)(s_dyn + a.brick_smem / 4) + warp * 32 * kStencilWords;  // this warp's staged stencils
+    for (int k = tid; k < P0 * P1 * P2; k += kBrickThreads) acc[k] = 0;
+    __syncthreads();
+    const int b0 = lane / kOrder, c0 = lane % kOrder;
+    for (int base = jbegin; base < R.block_end; base += kSpreadChunk) {
+        // 1. blocks whose bounding box reaches the brick, in block order
         const int J = base + tid;
+        int ent0 = -1, ent1 = -1;
         if (J < R.block_end) {
             if (g == 0) {
-                if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = J << 2;
+                if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e)) ent0 = J << 2;
             } else if (a.full) {
-                if (box_meets_brick(a.bb_c2[J], a.bb_h2[J], R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 2;
+                if (box_meets_brick(a.bb_c2[J], a.bb_h2[J], R, o, e)) ent0 = (J << 2) | 2;
             } else if (a.block_cls[J] != 0) {
                 const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
                 const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
-                if (box_meets_brick(c1, h1, R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 1;
-                if (box_meets_brick(c2, h1, R, o, e)) s_cand[atomicAdd(&s_ncand, 1)] = (J << 2) | 3;
+                if (box_meets_brick(c1, h1, R, o, e)) ent0 = (J << 2) | 1;
+                if (box_meets_brick(c2, h1, R, o, e)) ent1 = (J << 2) | 3;
+            }
+        }
+        const unsigned m0 = __ballot_sync(FULL_MASK, ent0 >= 0), m1 = __ballot_sync(FULL_MASK, ent1 >= 0);
+        if (lane == 0) s_wcount[warp] = __popc(m0) + __popc(m1);
+        __syncthreads();
+        int off = 0, nc = 0;
+#pragma unroll
+        for (int q = 0; q < kBrickWarps; q++) {
+            const int cq = s_wcount[q];
+            off += q < warp ? cq : 0;
+            nc += cq;
+        }
+        {
+            const unsigned lt = (1u << lane) - 1u;
+            int pos = off + __popc(m0 & lt) + __popc(m1 & lt);
+            if (ent0 >= 0) s_cand[pos++] = ent0;
+            if (ent1 >= 0) s_cand[pos] = ent1;
+        }
+        __syncthreads();
+        // 2. warp w takes candidates w, w + 8, ...: lanes = the block's atoms
+        for (int ci = warp; ci < nc; ci += kBrickWarps) {
+            const int ent = s_cand[ci];
+            const int Jc = ent >> 2, code = ent & 3;
+            const int s = Jc * kTile + lane;
+            const int nreal = __float_as_int(a.bb_h[Jc].w);
+            float4 p = code == 2 ? a.posq2[s] : a.posq[s];
+            const float4 dd = a.displ[s];
+            if (code == 1) p.w = -p.w;
+            if (code == 3) {
+                p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
+                p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
+                p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
+            }
+            bool ok = lane < nreal && p.w != 0.0f;
+            int lb[3];
+            if (ok) {
+                const float cc[3] = {p.x, p.y, p.z};
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    float f = cc[d] * R.ibox[d];
+                    f -= floorf(f);
+                    int bs = (int)floorf(f * (float)R.K[d]);
+                    if (bs >= R.K[d]) bs -= R.K[d];
+                    int v = bs - o[d];
+                    v += v < 0 ? R.K[d] : 0;
+                    ok = ok && v < e[d] + kOrder - 1;
+                    lb[d] = v + pad;  // local index of the stencil's top point (padded copy)
+                }
+            }
+            if (ok) {
+                Stencil S;
+                make_stencil(p.x, p.y, p.z, R, S, false);
+                float* w = st + lane * kStencilWords;
+                const float qs = p.w * kGridScale;
+#pragma unroll
+                for (int k = 0; k < kOrder; k++) {
+                    w[k] = qs * S.w[0][k];
+                    w[kOrder + k] = S.w[1][k];
+                    w[2 * kOrder + k] = S.w[2][k];
+                }
+                w[15] = __int_as_float(padded ? ((lb[0] << 20) | (lb[1] << 10) | lb[2])
+                                              : ((S.base[0] << 20) | (S.base[1] << 10) | S.base[2]));
+            }
+            unsigned bal = __ballot_sync(FULL_MASK, ok);
+            __syncwarp();
+            // 3. the listed atoms one by one, lanes over the 5 x 5 (y, z) offsets
+            while (bal) {
+                const int src = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const float* w = st + src * kStencilWords;
+                if (lane < kOrder * kOrder) {
+                    const int bases = __float_as_int(w[15]);
+                    const float wyz = w[kOrder + b0] * w[2 * kOrder + c0];
+                    if (padded) {
+                        const int ly = ((bases >> 10) & 1023) - b0, lz = (bases & 1023) - c0;
+                        const int row = ly * P2 + lz, lx0 = bases >> 20;
+#pragma unroll
+                        for (int a0 = 0; a0 < kOrder; a0++)
+                            atomicAdd(&acc[(lx0 - a0) * P1 * P2 + row], __float2int_rn(w[a0] * wyz));
+                    } else {
+                        const int ly = brick_local((bases >> 10) & 1023, b0, o[1], e[1], R.K[1]);
+                        const int lz = brick_local(bases & 1023, c0, o[2], e[2], R.K[2]);
+                        if (ly >= 0 && lz >= 0) {
+                            const int bx = bases >> 20;
+#pragma unroll
+                            for (int a0 = 0; a0 < kOrder; a0++) {
+                                const int lx = brick_local(bx, a0, o[0], e[0], R.K[0]);
+                                if (lx >= 0) atomicAdd(&acc[(lx * P1 + ly) * P2 + lz], __float2int_rn(w[a0] * wyz));
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
             }
         }
         __syncthreads();
-        const int nc = s_ncand;
-        for (int cb = 0; cb < nc; cb += kSpreadBatch) {
-            if (tid == 0) s_nlist = 0;
-            __syncthreads();
-            // 2. atoms of those blocks whose stencil reaches the brick (lanes = atoms)
-            const int ce = min(nc, cb + kSpreadBatch);
-            for (int ci = cb + warp; ci < ce; ci += kBrickThreads / 32) {
-                const int ent = s_cand[ci];
-                const int Jc = ent >> 2, code = ent & 3;
-                const int s = Jc * kTile + lane;
-                bool ok = lane < __float_as_int(a.bb_h[Jc].w);
-                if (ok) {
-                    const float4 p = entry_atom(a, R, s, code);
-                    ok = p.w != 0.0f;
-                    const float cc[3] = {p.x, p.y, p.z};
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        float f = cc[d] * R.ibox[d];
-                        f -= floorf(f);
-                        int bs = (int)floorf(f * (float)R.K[d]);
-                        if (bs >= R.K[d]) bs -= R.K[d];
-                        int v = bs - o[d];
-                        v += v < 0 ? R.K[d] : 0;
-                        ok = ok && v < e[d] + kOrder - 1;
-                    }
-                }
-                const unsigned bal = __ballot_sync(FULL_MASK, ok);
-                int pos = 0;
-                if (lane == 0 && bal) pos = atomicAdd(&s_nlist, __popc(bal));
-                pos = __shfl_sync(FULL_MASK, pos, 0);
-                if (ok) {
-                    // each listed atom's stencil, computed once: q*wx, wy, wz and
-                    // the brick-local indices of its first stencil point
-                    const int li = pos + __popc(bal & ((1u << lane) - 1u));
-                    const float4 p = entry_atom(a, R, s, code);
-                    Stencil S;
-                    make_stencil(p.x, p.y, p.z, R, S, false);
-                    float* wv = s_w + li * kStencilFloats;
-#pragma unroll
-                    for (int k = 0; k < kOrder; k++) {
-                        wv[k] = p.w * S.w[0][k];
-                        wv[kOrder + k] = S.w[1][k];
-                        wv[2 * kOrder + k] = S.w[2][k];
-                    }
-                    s_list[li] = (S.base[0] << 20) | (S.base[1] << 10) | S.base[2];
-                }
-            }
-            __syncthreads();
-            // 3. one atom per warp, lanes over the 5 x 5 (y, z) stencil offsets
-            const int nl = s_nlist;
-            const int b0 = lane / kOrder, c0 = lane % kOrder;
-            for (int li = warp; li < nl; li += kBrickThreads / 32) {
-                if (lane >= kOrder * kOrder) continue;
-                const int bases = s_list[li];
-                const float* wv = s_w + li * kStencilFloats;
-                const int ly = brick_local((bases >> 10) & 1023, b0, o[1], e[1], R.K[1]);
-                const int lz = brick_local(bases & 1023, c0, o[2], e[2], R.K[2]);
-                if (ly < 0 || lz < 0) continue;
-                const float wy = wv[kOrder + b0], wz = wv[2 * kOrder + c0];
-                const int bx = bases >> 20;
-#pragma unroll
-                for (int a0 = 0; a0 < kOrder; a0++) {
-                    const int lx = brick_local(bx, a0, o[0], e[0], R.K[0]);
-                    if (lx < 0) continue;
-                    const float v = wv[a0] * wy * wz;
-                    const long long q64 = __float2ll_rn(v * kFixScaleF);
-                    const int idx = (lx * e[1] + ly) * e[2] + lz;
-                    atomicAdd(&s_hi[idx], (int)(q64 >> 16));
-                    atomicAdd(&s_lo[idx], (unsigned)(q64 & 0xffff));
-                }
-            }
-            __syncthreads();
-        }
     }
-    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
-    float* G = a.qreal + R.real_off + (size_t)g * G3;
+    // 4. the brick's own points, each written once
     for (int k = tid; k < npts; k += kBrickThreads) {
         const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
-        const long long v = (long long)s_hi[k] * 65536ll + (long long)s_lo[k];
-        G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = (float)((double)v * (1.0 / kFixScale));
+        const int v = acc[((lx + pad) * P1 + ly + pad) * P2 + lz + pad];
+        G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = (float)v * (1.0f / kGridScale);
     }
 }
 

@@ -153,7 +153,8 @@ def test_autotune_keeps_parity(tmp_path, monkeypatch):
     report = b.autotune(trials=2, use_cache=False)
     assert "chosen:" in report and report.count("ms") >= 3
     E1, F1, r1 = b.evaluate(pos)
-    np.testing.assert_allclose(F1, F0, rtol=0, atol=1e-5)
+    # every tuning gives the same bits: forces and the PME grid are integer sums
+    assert np.array_equal(F1, F0)
     for k, c in enumerate(cases):
         ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
         assert abs(r1[k]["pert"] - ref["usc"]) <= U_TOL
