@@ -316,8 +316,11 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
 }
 
 // The 32 steps of one tile: lane l meets j-slot (l+k)&31 at step k; j data are
-// read from shared memory, j forces travel with their slot by warp shuffles.
-template <int METHOD, bool PBC, bool DIFF>
+// read from shared memory (stored twice over, so that slot (l+k)&31 is entry l+k
+// of the lane's own base: a constant offset per unrolled step), j forces travel
+// with their slot by warp shuffles.  MASKED: a per-lane bit mask of the pairs to
+// count (exclusions, padding); unmasked tiles park their padding j slots far away.
+template <int METHOD, bool PBC, bool DIFF, bool MASKED>
 __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
                                            float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
                                            float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
@@ -325,9 +328,8 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
     const int src = (lane + 1) & 31;
 #pragma unroll 8
     for (int k = 0; k < 32; k++) {
-        const int jl = (lane + k) & 31;
-        const float4 pj = sp[jl];
-        const float2 lj = sl[jl];
+        const float4 pj = sp[k];
+        const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         if (PBC) {
             dx = min_img(dx, Lx, iLx);
@@ -335,7 +337,7 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
             dz = min_img(dz, Lz, iLz);
         }
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const bool inc = ((mask >> k) & 1u) && r2 < rc2;
+        const bool inc = MASKED ? (((mask >> k) & 1u) && r2 < rc2) : r2 < rc2;
         float e, fr;
         pair_eval<METHOD>(inc ? r2 : 1.0f, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
         e = inc ? e : 0.0f;
@@ -366,9 +368,8 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
     const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
 #pragma unroll 4
     for (int k = 0; k < 32; k++) {
-        const int jl = (lane + k) & 31;
-        const float4 pj = sp[jl];
-        const float2 lj = sl[jl];
+        const float4 pj = sp[k];
+        const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         if (PBC) {
             dx = min_img(dx, Lx, iLx);
@@ -417,8 +418,8 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
 
 template <int METHOD>
 __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
-    __shared__ float4 s_p[kTileThreads / 32][32];
-    __shared__ float2 s_l[kTileThreads / 32][32];
+    __shared__ float4 s_p[kTileThreads / 32][64];
+    __shared__ float2 s_l[kTileThreads / 32][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -476,9 +477,17 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
             pi.y = c.y + min_img(pi.y - c.y, Ly, iLy);
             pi.z = c.z + min_img(pi.z - c.z, Lz, iLz);
         }
+        // atom tiles without per-pair minimum images need no mask: padding j slots
+        // are parked far beyond the cutoff
+        const bool masked = !atom_tile || pbc;
+        if (!masked && !jvalid) pj.x = pj.y = pj.z = 1.0e15f;
         s_p[w][lane] = pj;
+        s_p[w][lane + 32] = pj;
         s_l[w][lane] = lj;
+        s_l[w][lane + 32] = lj;
         __syncwarp();
+        const float4* spl = &s_p[w][lane];
+        const float2* sll = &s_l[w][lane];
         float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
         float3 ai = make_float3(0.f, 0.f, 0.f), aj = make_float3(0.f, 0.f, 0.f);
         float e32 = 0.f;
@@ -486,25 +495,31 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         const bool adj = diff && a.adjoint;
         if (adj) {
             if (pbc)
-                tile_steps_adj<METHOD, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                             alpha, krf, crf, fi, fj, e64, ai, aj);
+                tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
+                                             crf, fi, fj, e64, ai, aj);
             else
-                tile_steps_adj<METHOD, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                              alpha, krf, crf, fi, fj, e64, ai, aj);
+                tile_steps_adj<METHOD, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
+                                              crf, fi, fj, e64, ai, aj);
         } else if (diff) {
             if (pbc)
-                tile_steps<METHOD, true, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                               alpha, krf, crf, fi, fj, e32, e64);
+                tile_steps<METHOD, true, true, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                     alpha, krf, crf, fi, fj, e32, e64);
+            else if (masked)
+                tile_steps<METHOD, false, true, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                      alpha, krf, crf, fi, fj, e32, e64);
             else
-                tile_steps<METHOD, false, true>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                                alpha, krf, crf, fi, fj, e32, e64);
+                tile_steps<METHOD, false, true, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                       alpha, krf, crf, fi, fj, e32, e64);
         } else {
             if (pbc)
-                tile_steps<METHOD, true, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                                alpha, krf, crf, fi, fj, e32, e64);
+                tile_steps<METHOD, true, false, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                      alpha, krf, crf, fi, fj, e32, e64);
+            else if (masked)
+                tile_steps<METHOD, false, false, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                       alpha, krf, crf, fi, fj, e32, e64);
             else
-                tile_steps<METHOD, false, false>(s_p[w], s_l[w], pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
-                                                 alpha, krf, crf, fi, fj, e32, e64);
+                tile_steps<METHOD, false, false, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                                                        alpha, krf, crf, fi, fj, e32, e64);
         }
         __syncwarp();
         const bool diag = !atom_tile && T.y == I;
