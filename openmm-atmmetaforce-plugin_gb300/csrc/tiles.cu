@@ -189,17 +189,22 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int I, 
         const bool valid = k < natom;
         const int j = valid ? list[k] : 0;
         bool hit = false;
+        float4 p = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);  // invalid lanes never hit
         if (valid) {
-            float4 p = row_pos(a, kind, j);
+            p = row_pos(a, kind, j);
             p.x = ci.x + min_img(p.x - ci.x, R.box[0], R.ibox[0]);
             p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
             p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
-#pragma unroll 8
-            for (int q = 0; q < 32; q++) {
+        }
+        // eight i atoms at a time; stop once every lane has decided
+        for (int q0 = 0; q0 < 32; q0 += 8) {
+#pragma unroll
+            for (int q = q0; q < q0 + 8; q++) {
                 const float4 o = s_ipos[q];
                 const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
                 hit |= dx * dx + dy * dy + dz * dz < rc2;
             }
+            if (__all_sync(FULL_MASK, hit || !valid)) break;
         }
         __syncwarp();
         const bool keep = valid && hit;
@@ -523,9 +528,19 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         }
         __syncwarp();
         const bool diag = !atom_tile && T.y == I;
-        double esum = diff ? e64 : (double)e32 * (diag ? 0.5 : 1.0);
+        // tile energy: FP64 on the difference tiles (their sum is u), FP32 over the
+        // lanes otherwise (FP64 arithmetic is scarce on this part); fixed order either way
+        double esum;
+        if (diff) {
+            esum = e64;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+            for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+        } else {
+            float es = diag ? 0.5f * e32 : e32;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
+            esum = (double)es;
+        }
         const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
         if (lane == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
         unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
