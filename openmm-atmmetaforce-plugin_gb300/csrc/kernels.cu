@@ -699,6 +699,76 @@ __device__ __forceinline__ void gather_two(const float* G1, const float* G2, con
     if (pot2) *pot2 = ph2;
 }
 
+__device__ __forceinline__ float pick5(const float* w, int k) {
+    return k == 0 ? w[0] : k == 1 ? w[1] : k == 2 ? w[2] : k == 3 ? w[3] : k == 4 ? w[4] : 0.0f;
+}
+
+// Gradients of NG grids at one stencil with 16-byte loads: the five z points
+// base - 4 .. base of every (x, y) row lie in the aligned eight-float window that
+// starts at az = (base - 4) & ~3, read as two float4; the z weights are re-indexed
+// into that window once.  Returns false (nothing computed) when the window would
+// wrap around the grid; grids must start 16-byte aligned with Kz a multiple of 4.
+template <int NG>
+__device__ __forceinline__ bool gather_vec(const float* G0, const float* G1, const RepDev& R, const Stencil& S,
+                                           float* g0, float* g1, float* pot1) {
+    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
+    const int z0 = S.base[2] - (kOrder - 1);
+    const int az = z0 & ~3;
+    if (z0 < 0 || az + 8 > Kz) return false;
+    const int m = z0 - az;  // 0..3
+    float Wz[8], dWz[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int c = m + kOrder - 1 - k;  // z weight index of window entry k (-1..7 outside)
+        Wz[k] = pick5(S.w[2], c);
+        dWz[k] = pick5(S.dw[2], c);
+    }
+    float a0x = 0.f, a0y = 0.f, a0z = 0.f, a1x = 0.f, a1y = 0.f, a1z = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int i0 = 0; i0 < kOrder; i0++) {
+        int ix = S.base[0] - i0;
+        if (ix < 0) ix += Kx;
+#pragma unroll
+        for (int j0 = 0; j0 < kOrder; j0++) {
+            int iy = S.base[1] - j0;
+            if (iy < 0) iy += Ky;
+            const size_t ro = ((size_t)ix * Ky + iy) * Kz + az;
+            const float dxy = S.dw[0][i0] * S.w[1][j0], xdy = S.w[0][i0] * S.dw[1][j0], xy = S.w[0][i0] * S.w[1][j0];
+            {
+                const float4 lo = __ldg((const float4*)(G0 + ro)), hi = __ldg((const float4*)(G0 + ro + 4));
+                const float sx = Wz[0] * lo.x + Wz[1] * lo.y + Wz[2] * lo.z + Wz[3] * lo.w + Wz[4] * hi.x +
+                                 Wz[5] * hi.y + Wz[6] * hi.z + Wz[7] * hi.w;
+                const float sz = dWz[0] * lo.x + dWz[1] * lo.y + dWz[2] * lo.z + dWz[3] * lo.w + dWz[4] * hi.x +
+                                 dWz[5] * hi.y + dWz[6] * hi.z + dWz[7] * hi.w;
+                a0x += dxy * sx;
+                a0y += xdy * sx;
+                a0z += xy * sz;
+            }
+            if (NG == 2) {
+                const float4 lo = __ldg((const float4*)(G1 + ro)), hi = __ldg((const float4*)(G1 + ro + 4));
+                const float sx = Wz[0] * lo.x + Wz[1] * lo.y + Wz[2] * lo.z + Wz[3] * lo.w + Wz[4] * hi.x +
+                                 Wz[5] * hi.y + Wz[6] * hi.z + Wz[7] * hi.w;
+                const float sz = dWz[0] * lo.x + dWz[1] * lo.y + dWz[2] * lo.z + dWz[3] * lo.w + dWz[4] * hi.x +
+                                 dWz[5] * hi.y + dWz[6] * hi.z + dWz[7] * hi.w;
+                a1x += dxy * sx;
+                a1y += xdy * sx;
+                a1z += xy * sz;
+                p1 += xy * sx;
+            }
+        }
+    }
+    g0[0] = a0x;
+    g0[1] = a0y;
+    g0[2] = a0z;
+    if (NG == 2) {
+        g1[0] = a1x;
+        g1[1] = a1y;
+        g1[2] = a1z;
+        if (pot1) *pot1 = p1;
+    }
+    return true;
+}
+
 __device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, int s, float q, float gx, float gy,
                                                float gz, const RepDev& R) {
     fix_add(F + s, -q * gx * (float)R.K[0] * R.ibox[0]);
@@ -708,7 +778,7 @@ __device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, in
 
 // Reciprocal-space forces of every atom that does not move (difference mode)
 // or of every atom at both states (two-state mode).
-__global__ void __launch_bounds__(128, 6) k_gather(Args a) {
+__global__ void __launch_bounds__(128, 5) k_gather(Args a) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.NA) return;
     const int b = s >> 5;
@@ -733,7 +803,9 @@ __global__ void __launch_bounds__(128, 6) k_gather(Args a) {
     } else {
         // F1 from the state-1 potential; F2 - F1 from the potential of the moved charges
         float g1[3], g2[3], pot2 = 0.f;
-        gather_two(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr);
+        const bool vec = ((R.real_off | (long long)R.K[2]) & 3) == 0;
+        if (!(vec && gather_vec<2>(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr)))
+            gather_two(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr);
         add_grad_force(a.F, a.NA, s, p.w, g1[0], g1[1], g1[2], R);
         add_grad_force(F2, a.NA, s, p.w, g2[0], g2[1], g2[2], R);
         if (a.adjoint) fix_add(a.D + s, pot2);  // d(E2 - E1)_rec / d(scaled charge)
