@@ -477,6 +477,7 @@ void Engine::build_layout() {
             rd.box[a] = (float)s.box[a];
             rd.ibox[a] = (float)(1.0 / s.box[a]);
             rd.boxd[a] = s.box[a];
+            rd.iboxd[a] = 1.0 / s.box[a];
             rd.K[a] = s.grid[a];
         }
         double q2 = 0;
@@ -802,6 +803,7 @@ void Engine::alloc_device() {
     a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
     a.tile_j = dalloc<int>(d_allocs_, 32 * (size_t)tile_cap_);
     a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
+    a.e_row = dalloc<double>(d_allocs_, (size_t)nrows_);
     a.status = dalloc<Status>(d_allocs_, 1);
     a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);
     a.adjoint = adjoint_ ? 1 : 0;
@@ -861,6 +863,7 @@ void Engine::update_rep_table() {
             rd.box[a] = (float)s.box[a];
             rd.ibox[a] = (float)(1.0 / s.box[a]);
             rd.boxd[a] = s.box[a];
+            rd.iboxd[a] = 1.0 / s.box[a];
         }
         for (int k = 0; k < NUM_GLOBALS; k++) rd.params[k] = s.params[k];
         rd.e_disp = s.dispersion ? dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]) : 0.0;
@@ -874,8 +877,8 @@ void Engine::update_rep_table() {
 // ---------------------------------------------------------------------------
 
 int Engine::launches_per_eval() const {
-    // prepare, find, tiles, exceptions, finalize, output, matrix (+ PME kernels)
-    int n = 4 + 3;
+    // prepare, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)
+    int n = 4 + 4;
     if (method_ == NonbondedForce::PME) n += 3;  // spread, conv, gather
     if (method_ == NonbondedForce::PME && !full_) {
         bool any = false;

@@ -76,9 +76,9 @@ __global__ void k_prepare(Args a) {
     const int nreal = __popc(__ballot_sync(FULL_MASK, o >= 0));  // padding sits at the end of a block
     if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
     const double* p = a.pos_in + 3 * (size_t)(R.in_off + o);
-    float x = (float)(p[0] - R.boxd[0] * floor(p[0] / R.boxd[0]));
-    float y = (float)(p[1] - R.boxd[1] * floor(p[1] / R.boxd[1]));
-    float z = (float)(p[2] - R.boxd[2] * floor(p[2] / R.boxd[2]));
+    float x = (float)(p[0] - R.boxd[0] * floor(p[0] * R.iboxd[0]));
+    float y = (float)(p[1] - R.boxd[1] * floor(p[1] * R.iboxd[1]));
+    float z = (float)(p[2] - R.boxd[2] * floor(p[2] * R.iboxd[2]));
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
     for (int k = 0; k < 6; k++) a.F[(size_t)k * a.NA + s] = 0ull;
@@ -142,9 +142,9 @@ __device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const
     f[2] = fr * dz;
     if (a.method == 4) {
         // Ewald exclusion correction at the minimum-image separation
-        double mx = dx - R.boxd[0] * rint(dx / R.boxd[0]);
-        double my = dy - R.boxd[1] * rint(dy / R.boxd[1]);
-        double mz = dz - R.boxd[2] * rint(dz / R.boxd[2]);
+        double mx = dx - R.boxd[0] * rint(dx * R.iboxd[0]);
+        double my = dy - R.boxd[1] * rint(dy * R.iboxd[1]);
+        double mz = dz - R.boxd[2] * rint(dz * R.iboxd[2]);
         double m2 = mx * mx + my * my + mz * mz;
         if (m2 > 0.0) {
             double r = sqrt(m2);
@@ -917,13 +917,22 @@ __device__ double block_sum(double v, double* sh) {
     return r;
 }
 
+// Energy of each tile row, one warp per row (lanes over the row's slots, fixed order).
+__global__ void k_rowsum(Args a) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= a.nrows) return;
+    const int n = a.row_count[row];
+    const double* e = a.e_tile + (size_t)row * a.row_cap;
+    double s = 0.0;
+    for (int k = lane; k < n; k += 32) s += e[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+    if (lane == 0) a.e_row[row] = s;
+}
+
 __device__ double rows_sum(const Args& a, int rb, int re) {
     double s = 0.0;
-    for (int row = rb + threadIdx.x; row < re; row += blockDim.x) {
-        int n = a.row_count[row];
-        const double* e = a.e_tile + (size_t)row * a.row_cap;
-        for (int k = 0; k < n; k++) s += e[k];
-    }
+    for (int row = rb + threadIdx.x; row < re; row += blockDim.x) s += a.e_row[row];
     return s;
 }
 
@@ -966,6 +975,7 @@ __global__ void __launch_bounds__(256) k_finalize(Args a) {
 }
 
 void launch_finalize(const Args& a, cudaStream_t s) {
+    k_rowsum<<<(a.nrows * 32 + 255) / 256, 256, 0, s>>>(a);
     k_finalize<<<a.R, 256, 0, s>>>(a);
 }
 

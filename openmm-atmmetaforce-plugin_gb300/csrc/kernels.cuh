@@ -32,6 +32,7 @@ struct RepDev {
     float box[4];      // L (x,y,z), unused
     float ibox[4];     // 1/L
     double boxd[3];
+    double iboxd[3];          // 1/L in FP64 (FP64 division is slow on this part)
     int slot_begin, slot_end;
     int block_begin, block_end;
     int mov_block_begin;      // first moving block (== block_end when none)
@@ -113,6 +114,7 @@ struct Args {
     int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
     int* tile_j;              // 32 j slots per tile (atom tiles)
     double* e_tile;           // nrows*row_cap
+    double* e_row;            // nrows: sum of each row's tiles
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]
     unsigned long long* F;
