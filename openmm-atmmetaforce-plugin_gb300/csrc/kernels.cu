@@ -208,9 +208,10 @@ __device__ __forceinline__ float exc_term_f(const Args& a, const RepDev& R, cons
 }
 
 __global__ void __launch_bounds__(256) k_exceptions(Args a) {
-    __shared__ double red[3][256];
+    __shared__ double red[3][8];
     int c = blockIdx.x;
     int e = a.exc_cta_first[c] + threadIdx.x;
+    float E1f = 0.0f;  // same-class pairs (FP32 terms, summed in FP32 within a warp)
     double E1 = 0.0, E2 = 0.0, DE = 0.0;
     if (e < a.exc_cta_first[c + 1]) {
         int4 ij = a.exc_ij[e];
@@ -218,25 +219,23 @@ __global__ void __launch_bounds__(256) k_exceptions(Args a) {
         const RepDev& R = a.reps[ij.z];
         const double* xi = a.pos_in + 3 * (size_t)ij.x;
         const double* xj = a.pos_in + 3 * (size_t)ij.y;
-        const double* di = a.displ_in + 3 * (size_t)ij.x;
-        const double* dj = a.displ_in + 3 * (size_t)ij.y;
         int si = a.slot_of[ij.x], sj = a.slot_of[ij.y];
         if (!ij.w) {
             float g[3];
-            float e1 = exc_term_f(a, R, p, (float)(xj[0] - xi[0]), (float)(xj[1] - xi[1]), (float)(xj[2] - xi[2]), g);
-            E1 = (double)e1;
+            E1f = exc_term_f(a, R, p, (float)(xj[0] - xi[0]), (float)(xj[1] - xi[1]), (float)(xj[2] - xi[2]), g);
             for (int k = 0; k < 3; k++) {
-                fix_add_d(a.F + (size_t)k * a.NA + si, -(double)g[k]);
-                fix_add_d(a.F + (size_t)k * a.NA + sj, (double)g[k]);
+                fix_add(a.F + (size_t)k * a.NA + si, -g[k]);
+                fix_add(a.F + (size_t)k * a.NA + sj, g[k]);
             }
             if (a.full) {
-                E2 = E1;
                 for (int k = 0; k < 3; k++) {
-                    fix_add_d(a.F + (size_t)(3 + k) * a.NA + si, -(double)g[k]);
-                    fix_add_d(a.F + (size_t)(3 + k) * a.NA + sj, (double)g[k]);
+                    fix_add(a.F + (size_t)(3 + k) * a.NA + si, -g[k]);
+                    fix_add(a.F + (size_t)(3 + k) * a.NA + sj, g[k]);
                 }
             }
         } else {
+            const double* di = a.displ_in + 3 * (size_t)ij.x;
+            const double* dj = a.displ_in + 3 * (size_t)ij.y;
             double f1[3], f2[3], g1, g2;
             E1 = exc_term(a, R, p, xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2], f1, &g1);
             for (int k = 0; k < 3; k++) {
@@ -261,16 +260,31 @@ __global__ void __launch_bounds__(256) k_exceptions(Args a) {
             }
         }
     }
-    red[0][threadIdx.x] = E1;
-    red[1][threadIdx.x] = E2;
-    red[2][threadIdx.x] = DE;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o)
-            for (int k = 0; k < 3; k++) red[k][threadIdx.x] += red[k][threadIdx.x + o];
-        __syncthreads();
+    // fixed-order sums: FP32 same-class terms within the warp, FP64 from there on;
+    // in two-state mode the same-class terms enter both states identically
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) E1f += __shfl_xor_sync(FULL_MASK, E1f, o);
+    const bool any_cross = __any_sync(FULL_MASK, E1 != 0.0 || E2 != 0.0 || DE != 0.0);
+    if (any_cross) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            E1 += __shfl_xor_sync(FULL_MASK, E1, o);
+            E2 += __shfl_xor_sync(FULL_MASK, E2, o);
+            DE += __shfl_xor_sync(FULL_MASK, DE, o);
+        }
     }
-    if (threadIdx.x < 3) a.e_part_exc[3 * c + threadIdx.x] = red[threadIdx.x][0];
+    if (lane == 0) {
+        red[0][w] = E1 + (double)E1f;
+        red[1][w] = E2 + (a.full ? (double)E1f : 0.0);
+        red[2][w] = DE;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int q = 0; q < 8; q++) t += red[threadIdx.x][q];
+        a.e_part_exc[3 * c + threadIdx.x] = t;
+    }
 }
 
 void launch_exceptions(const Args& a, cudaStream_t s) {
