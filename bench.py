@@ -29,8 +29,11 @@ METRIC = "ATM evals/sec/replica at 23.5k-atom PME: batched vs plain on one GB300
 F_PAIR = 55.0  # FP32 flops per pair (accounting constant)
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) of one k_tiles launch on this workload, from an ncu
-# --set full capture (78.50 MB read + 2.85 MB write)
-TILES_TRAFFIC_BYTES = 81.34e6
+# --set full capture (65.22 MB read + 1.70 MB write)
+TILES_TRAFFIC_BYTES = 66.92e6
+# warp instructions of one k_tiles launch on this workload (same capture): the
+# kernel is issue-bound, so its issue rate is the second roofline reported
+TILES_WARP_INSTR = 623.9e6
 
 
 def parse():
@@ -366,7 +369,12 @@ def main():
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
                 "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt, "tile_stats": batch.stats(),
-                "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 1024 * batch.stats()["tiles"])}
+                "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 1024 * batch.stats()["tiles"]),
+                "issue": {"achieved": TILES_WARP_INSTR / t_tiles / 1e12,
+                          "peak": props.multi_processor_count * 4 * sm_mhz * 1e6 / 1e12,
+                          "unit": "T warp instructions/s",
+                          "frac": TILES_WARP_INSTR / t_tiles / (props.multi_processor_count * 4 * sm_mhz * 1e6),
+                          "source": "instructions per launch from the ncu capture, kernel time live"}}
 
     md = None
     if not args.no_md:
