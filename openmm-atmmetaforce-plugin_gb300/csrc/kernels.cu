@@ -381,6 +381,7 @@ __device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev
 }
 
 constexpr int kSpreadChunk = kBrickThreads;  // blocks examined per pass (one per thread)
+constexpr int kSpreadCandCap = 2048;         // candidate entries listed before they are added
 constexpr int kStencilWords = 16;            // q*wx[5], wy[5], wz[5], packed bases
 
 // Dynamic shared memory of a spreading CTA: the brick accumulator (accum_bytes)
@@ -395,9 +396,91 @@ __device__ __forceinline__ int brick_local(int base, int k, int o, int e, int K)
     return v < e ? v : -1;
 }
 
+// Adds the stencils of the atoms of candidate blocks s_cand[0 .. nc) to the brick
+// accumulator: warp w takes candidates w, w + 8, ...; lanes = the block's atoms.
+__device__ __forceinline__ void spread_candidates(const Args& a, const RepDev& R, const int* s_cand, int nc, int warp,
+                                                  int lane, const int* o, const int* e, int pad, bool padded, int P1,
+                                                  int P2, int* acc, float* st, int b0, int c0) {
+    for (int ci = warp; ci < nc; ci += kBrickWarps) {
+        const int ent = s_cand[ci];
+        const int Jc = ent >> 2, code = ent & 3;
+        const int s = Jc * kTile + lane;
+        const int nreal = __float_as_int(a.bb_h[Jc].w);
+        float4 p = code == 2 ? a.posq2[s] : a.posq[s];
+        const float4 dd = a.displ[s];
+        if (code == 1) p.w = -p.w;
+        if (code == 3) {
+            p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
+            p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
+            p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
+        }
+        bool ok = lane < nreal && p.w != 0.0f;
+        int lb[3];
+        if (ok) {
+            const float cc[3] = {p.x, p.y, p.z};
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                float f = cc[d] * R.ibox[d];
+                f -= floorf(f);
+                int bs = (int)floorf(f * (float)R.K[d]);
+                if (bs >= R.K[d]) bs -= R.K[d];
+                int v = bs - o[d];
+                v += v < 0 ? R.K[d] : 0;
+                ok = ok && v < e[d] + kOrder - 1;
+                lb[d] = v + pad;  // local index of the stencil's top point (padded copy)
+            }
+        }
+        if (ok) {
+            Stencil S;
+            make_stencil(p.x, p.y, p.z, R, S, false);
+            float* w = st + lane * kStencilWords;
+            const float qs = p.w * kGridScale;
+#pragma unroll
+            for (int k = 0; k < kOrder; k++) {
+                w[k] = qs * S.w[0][k];
+                w[kOrder + k] = S.w[1][k];
+                w[2 * kOrder + k] = S.w[2][k];
+            }
+            w[15] = __int_as_float(padded ? ((lb[0] << 20) | (lb[1] << 10) | lb[2])
+                                          : ((S.base[0] << 20) | (S.base[1] << 10) | S.base[2]));
+        }
+        unsigned bal = __ballot_sync(FULL_MASK, ok);
+        __syncwarp();
+        // 3. the listed atoms one by one, lanes over the 5 x 5 (y, z) offsets
+        while (bal) {
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const float* w = st + src * kStencilWords;
+            if (lane < kOrder * kOrder) {
+                const int bases = __float_as_int(w[15]);
+                const float wyz = w[kOrder + b0] * w[2 * kOrder + c0];
+                if (padded) {
+                    const int ly = ((bases >> 10) & 1023) - b0, lz = (bases & 1023) - c0;
+                    const int row = ly * P2 + lz, lx0 = bases >> 20;
+#pragma unroll
+                    for (int a0 = 0; a0 < kOrder; a0++)
+                        atomicAdd(&acc[(lx0 - a0) * P1 * P2 + row], __float2int_rn(w[a0] * wyz));
+                } else {
+                    const int ly = brick_local((bases >> 10) & 1023, b0, o[1], e[1], R.K[1]);
+                    const int lz = brick_local(bases & 1023, c0, o[2], e[2], R.K[2]);
+                    if (ly >= 0 && lz >= 0) {
+                        const int bx = bases >> 20;
+#pragma unroll
+                        for (int a0 = 0; a0 < kOrder; a0++) {
+                            const int lx = brick_local(bx, a0, o[0], e[0], R.K[0]);
+                            if (lx >= 0) atomicAdd(&acc[(lx * P1 + ly) * P2 + lz], __float2int_rn(w[a0] * wyz));
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     extern __shared__ int s_dyn[];
-    __shared__ int s_cand[2 * kSpreadChunk];
+    __shared__ int s_cand[kSpreadCandCap];
     __shared__ int s_wcount[kBrickWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c = blockIdx.x;
@@ -444,6 +527,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     for (int k = tid; k < P0 * P1 * P2; k += kBrickThreads) acc[k] = 0;
     __syncthreads();
     const int b0 = lane / kOrder, c0 = lane % kOrder;
+    int ncand = 0;  // candidates listed and not yet added (the same in every thread)
     for (int base = jbegin; base < R.block_end; base += kSpreadChunk) {
         // 1. blocks whose bounding box reaches the brick, in block order
         const int J = base + tid;
@@ -470,91 +554,23 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
             off += q < warp ? cq : 0;
             nc += cq;
         }
+        if (ncand + nc > kSpreadCandCap) {  // list full: add what is listed first
+            spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0);
+            __syncthreads();
+            ncand = 0;
+        }
         {
             const unsigned lt = (1u << lane) - 1u;
-            int pos = off + __popc(m0 & lt) + __popc(m1 & lt);
+            int pos = ncand + off + __popc(m0 & lt) + __popc(m1 & lt);
             if (ent0 >= 0) s_cand[pos++] = ent0;
             if (ent1 >= 0) s_cand[pos] = ent1;
         }
-        __syncthreads();
-        // 2. warp w takes candidates w, w + 8, ...: lanes = the block's atoms
-        for (int ci = warp; ci < nc; ci += kBrickWarps) {
-            const int ent = s_cand[ci];
-            const int Jc = ent >> 2, code = ent & 3;
-            const int s = Jc * kTile + lane;
-            const int nreal = __float_as_int(a.bb_h[Jc].w);
-            float4 p = code == 2 ? a.posq2[s] : a.posq[s];
-            const float4 dd = a.displ[s];
-            if (code == 1) p.w = -p.w;
-            if (code == 3) {
-                p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
-                p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
-                p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
-            }
-            bool ok = lane < nreal && p.w != 0.0f;
-            int lb[3];
-            if (ok) {
-                const float cc[3] = {p.x, p.y, p.z};
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    float f = cc[d] * R.ibox[d];
-                    f -= floorf(f);
-                    int bs = (int)floorf(f * (float)R.K[d]);
-                    if (bs >= R.K[d]) bs -= R.K[d];
-                    int v = bs - o[d];
-                    v += v < 0 ? R.K[d] : 0;
-                    ok = ok && v < e[d] + kOrder - 1;
-                    lb[d] = v + pad;  // local index of the stencil's top point (padded copy)
-                }
-            }
-            if (ok) {
-                Stencil S;
-                make_stencil(p.x, p.y, p.z, R, S, false);
-                float* w = st + lane * kStencilWords;
-                const float qs = p.w * kGridScale;
-#pragma unroll
-                for (int k = 0; k < kOrder; k++) {
-                    w[k] = qs * S.w[0][k];
-                    w[kOrder + k] = S.w[1][k];
-                    w[2 * kOrder + k] = S.w[2][k];
-                }
-                w[15] = __int_as_float(padded ? ((lb[0] << 20) | (lb[1] << 10) | lb[2])
-                                              : ((S.base[0] << 20) | (S.base[1] << 10) | S.base[2]));
-            }
-            unsigned bal = __ballot_sync(FULL_MASK, ok);
-            __syncwarp();
-            // 3. the listed atoms one by one, lanes over the 5 x 5 (y, z) offsets
-            while (bal) {
-                const int src = __ffs(bal) - 1;
-                bal &= bal - 1;
-                const float* w = st + src * kStencilWords;
-                if (lane < kOrder * kOrder) {
-                    const int bases = __float_as_int(w[15]);
-                    const float wyz = w[kOrder + b0] * w[2 * kOrder + c0];
-                    if (padded) {
-                        const int ly = ((bases >> 10) & 1023) - b0, lz = (bases & 1023) - c0;
-                        const int row = ly * P2 + lz, lx0 = bases >> 20;
-#pragma unroll
-                        for (int a0 = 0; a0 < kOrder; a0++)
-                            atomicAdd(&acc[(lx0 - a0) * P1 * P2 + row], __float2int_rn(w[a0] * wyz));
-                    } else {
-                        const int ly = brick_local((bases >> 10) & 1023, b0, o[1], e[1], R.K[1]);
-                        const int lz = brick_local(bases & 1023, c0, o[2], e[2], R.K[2]);
-                        if (ly >= 0 && lz >= 0) {
-                            const int bx = bases >> 20;
-#pragma unroll
-                            for (int a0 = 0; a0 < kOrder; a0++) {
-                                const int lx = brick_local(bx, a0, o[0], e[0], R.K[0]);
-                                if (lx >= 0) atomicAdd(&acc[(lx * P1 + ly) * P2 + lz], __float2int_rn(w[a0] * wyz));
-                            }
-                        }
-                    }
-                }
-                __syncwarp();
-            }
-        }
+        ncand += nc;
         __syncthreads();
     }
+    // 2. all listed candidates at once (one barrier for the whole brick)
+    spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0);
+    __syncthreads();
     // 4. the brick's own points, each written once
     for (int k = tid; k < npts; k += kBrickThreads) {
         const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
