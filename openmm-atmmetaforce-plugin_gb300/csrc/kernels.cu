@@ -97,6 +97,7 @@ __global__ void k_prepare(Args a) {
         a.status->tile_count = 0;
         a.status->overflow = 0;
         a.status->max_row = 0;
+        a.status->next_tile = 0;
     }
 }
 

@@ -66,7 +66,7 @@ struct Status {
     int tile_count;   // tiles appended by the finder
     int overflow;     // bit 0: tile list, bit 1: row capacity
     int max_row;      // largest row seen
-    int pad;
+    int next_tile;    // work counter of the pair-tile kernel (tiles handed out)
 };
 
 // Arguments shared by the kernels of one engine (passed by value).

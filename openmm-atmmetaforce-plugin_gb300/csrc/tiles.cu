@@ -27,6 +27,7 @@ namespace atm {
 #define FULL_MASK 0xffffffffu
 
 constexpr int kFindWarps = 4;
+constexpr int kTileGrab = 4;  // tiles per grab of the pair-tile kernel
 
 __device__ __forceinline__ void fix_add_t(unsigned long long* p, float v) {
     atomicAdd(p, (unsigned long long)__float2ll_rn(v * kFixScaleF));
@@ -426,12 +427,18 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     __shared__ float4 s_p[kTileThreads / 32][64];
     __shared__ float2 s_l[kTileThreads / 32][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     int ntiles = a.status->tile_count;
     if (ntiles > a.tile_cap) ntiles = a.tile_cap;
     const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
-    for (int t = gw; t < ntiles; t += nw) {
+    // tiles are handed out kTileGrab at a time from a counter, the next grab
+    // requested before the current one is processed, so that warps finish together
+    int mine = 0;
+    if (lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+    int cur = __shfl_sync(FULL_MASK, mine, 0);
+    while (cur < ntiles) {
+    if (lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+    const int cur_end = min(cur + kTileGrab, ntiles);
+    for (int t = cur; t < cur_end; t++) {
         const int4 T = a.tiles[t];
         const int I = T.x;
         const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
@@ -563,6 +570,8 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
                 fix_add_t(D + 2 * (size_t)a.NA + j, sign * aj.z);
             }
         }
+    }
+    cur = __shfl_sync(FULL_MASK, mine, 0);
     }
 }
 
