@@ -98,6 +98,7 @@ __global__ void k_prepare(Args a) {
         a.status->overflow = 0;
         a.status->max_row = 0;
         a.status->next_tile = 0;
+        a.status->next_row = 0;
     }
 }
 

@@ -67,6 +67,8 @@ struct Status {
     int overflow;     // bit 0: tile list, bit 1: row capacity
     int max_row;      // largest row seen
     int next_tile;    // work counter of the pair-tile kernel (tiles handed out)
+    int next_row;     // work counter of the tile finder (rows handed out)
+    int pad[3];
 };
 
 // Arguments shared by the kernels of one engine (passed by value).

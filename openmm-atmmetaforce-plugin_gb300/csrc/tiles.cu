@@ -20,6 +20,8 @@
 //       aux  = mask id + 1 (block tiles) or number of valid j (atom tiles)
 //       slot = position of the tile within its row (energy slot)
 //       pbc  = 1 when every pair needs its own minimum image (small boxes)
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace atm {
@@ -217,14 +219,8 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int I, 
     return kept;
 }
 
-__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
-    __shared__ int s_stage[kFindWarps][kStageAtoms];
-    __shared__ float4 s_ipos[kFindWarps][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // last rows first: the state-2 / difference rows at the end of the row list
-    // scan every block of their replica and are the longest, so they start early
-    const int row = a.nrows - 1 - (blockIdx.x * kFindWarps + w);
-    if (row < 0) return;
+// The tiles of one row (one warp; stage and ipos: the warp's shared memory).
+__device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* stage, float4* ipos) {
     const int4 d = a.row_desc[row];
     const int I = d.x, kind = d.y;
     const RepDev& R = a.reps[d.z];
@@ -242,9 +238,9 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
                              ? 1u
                              : 0u;
     // staged in shared memory; rows longer than the stage are written by a second pass
-    int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, s_stage[w], kStageAtoms);
+    int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms);
     __syncwarp();
-    if (natom <= kStageAtoms && !pbc) natom = exact_cut(a, R, I, kind, ci, lane, s_stage[w], natom, s_ipos[w]);
+    if (natom <= kStageAtoms && !pbc) natom = exact_cut(a, R, I, kind, ci, lane, stage, natom, ipos);
     const int nblock = e1 - e0;
     const int natile = (natom + 31) / 32;
     int n = nblock + natile;
@@ -264,7 +260,7 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     }
     int* out = a.tile_j + (size_t)(tbase + nblock) * 32;
     if (natom <= kStageAtoms) {
-        for (int k = lane; k < natom; k += 32) out[k] = s_stage[w][k];
+        for (int k = lane; k < natom; k += 32) out[k] = stage[k];
     } else {
         // second pass: the same atoms, in the same order, straight into the j slots
         row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom);
@@ -282,8 +278,35 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     }
 }
 
+// Persistent: every warp takes rows from a counter, last rows first (the
+// state-2 / difference rows at the end of the row list scan every block of
+// their replica and are the longest, so they start early); the next row is
+// requested before the current one is built.
+__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
+    __shared__ int s_stage[kFindWarps][kStageAtoms];
+    __shared__ float4 s_ipos[kFindWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int mine = 0;
+    if (lane == 0) mine = atomicAdd(&a.status->next_row, 1);
+    int k = __shfl_sync(FULL_MASK, mine, 0);
+    while (k < a.nrows) {
+        if (lane == 0) mine = atomicAdd(&a.status->next_row, 1);
+        find_row(a, a.nrows - 1 - k, lane, s_stage[w], s_ipos[w]);
+        __syncwarp();
+        k = __shfl_sync(FULL_MASK, mine, 0);
+    }
+}
+
 void launch_find(const Args& a, cudaStream_t s) {
-    int blocks = (a.nrows + kFindWarps - 1) / kFindWarps;
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, kFindWarps * 32, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int blocks = std::min(per_sm * sms, (a.nrows + kFindWarps - 1) / kFindWarps);
     k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
 }
 
