@@ -305,11 +305,11 @@ def main():
     pos_pin = torch.from_numpy(pos_host).pin_memory().numpy()
     F_pin = torch.empty(pos_host.shape, dtype=torch.float64).pin_memory().numpy()
     for _ in range(args.warmup):
-        batch.evaluate(pos_pin, out=F_pin)
+        batch.evaluate(pos_pin, out=F_pin, as_array=True)
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        E, F, res = batch.evaluate(pos_pin, out=F_pin)
+        E, F, res = batch.evaluate(pos_pin, out=F_pin, as_array=True)
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(e2e_s, pg, dev)
     e2e_value = world * R / e2e_s

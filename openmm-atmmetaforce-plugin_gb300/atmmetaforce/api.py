@@ -460,13 +460,14 @@ class ReplicaBatch:
         a, b, c = _vec3(a), _vec3(b), _vec3(c)
         call("atm_batch_set_periodic_box_vectors", self._h, int(replica), _ptr(a), _ptr(b), _ptr(c))
 
-    def evaluate(self, positions=None, forces=True, out=None):
+    def evaluate(self, positions=None, forces=True, out=None, as_array=False):
         """Evaluate every replica.  positions: None (stored) or an array of
         shape (sum n, 3).  Returns (energies[R], forces[(sum n), 3] or None,
         results: list of dicts).  ``out``: a C-contiguous float64 (sum n, 3)
         array to receive the forces.  Page-locked buffers (e.g. from
         ``torch.empty(..., pin_memory=True).numpy()``) are copied to and from the
-        GPU directly, without a staging copy."""
+        GPU directly, without a staging copy.  ``as_array``: the results as an
+        (R, NUM_RES) array (columns in ``RES_KEYS`` order) instead of dicts."""
         pos = None
         if positions is not None:
             pos = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).reshape(-1, 3))
@@ -482,6 +483,8 @@ class ReplicaBatch:
         res = np.zeros((self.R, NUM_RES))
         call("atm_batch_evaluate", self._h, _ptr(pos) if pos is not None else None, _ptr(E),
              _ptr(F) if F is not None else None, _ptr(res))
+        if as_array:
+            return E, F, res
         return E, F, [dict(zip(RES_KEYS, row.tolist())) for row in res]
 
     def results_array(self, positions=None):

@@ -260,3 +260,21 @@ def test_update_parameters_in_context_and_no_moving_atoms():
     assert f.getPerturbationEnergy(ctx) == 0.0
     E1, F1, _ = O.nonbonded(c.spec, c.pos)
     assert force_rel(s.getForces(), F1) <= F_TOL
+
+
+def test_batch_results_array_matches_dicts_and_pinned_buffers():
+    import torch
+
+    cases = [S.abfe_pme_small(2000, 10, 33), S.abfe_pme_small(2000, 10, 34)]
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    pos = np.concatenate([c.pos for c in cases])
+    E, F, res = b.evaluate(pos)
+    # page-locked caller buffers are copied from and to directly
+    pos_pin = torch.from_numpy(pos).pin_memory().numpy()
+    F_pin = torch.empty(pos.shape, dtype=torch.float64).pin_memory().numpy()
+    E2, F2, arr = b.evaluate(pos_pin, out=F_pin, as_array=True)
+    assert F2 is F_pin
+    np.testing.assert_array_equal(F2, F)
+    np.testing.assert_array_equal(E2, E)
+    for k in range(len(cases)):
+        assert [res[k][key] for key in atm.RES_KEYS] == arr[k].tolist()
