@@ -272,6 +272,17 @@ int atm_md_get_state(atm_md_t md, double* pos, double* vel, double* forces, doub
 /* Steps taken, re-sorts made, and per replica degrees of freedom
  * (3 x particles with mass - constraints; dof nullable, R entries). */
 int atm_md_get_info(atm_md_t md, long long* steps, int* reorders, int* dof);
+/* No counterpart in the reference (its scripts read the perturbation energy from
+ * the context after each MD cycle, example/abfe/abfe.py:108-131).  Streaming of
+ * the thermodynamic data of the ATM replicas: every `interval` steps (0: off) the
+ * result records (R x ATM_NUM_RES: u, W, dW/dlambda1, dW/dlambda2, ...) and the
+ * R x R reduced-energy matrix at beta = 1/kT are copied on the device into a
+ * ring of `capacity` records, with no host synchronisation.  get_records copies
+ * the kept records oldest first (steps, results R x ATM_NUM_RES each, matrices
+ * R x R each; outputs nullable, sized for max_records) and empties the ring. */
+int atm_md_set_recording(atm_md_t md, int interval, int capacity);
+int atm_md_get_records(atm_md_t md, long long* steps, double* results, double* matrices, int max_records,
+                       int* n_records);
 
 /* ---- allocation-free variant ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc:

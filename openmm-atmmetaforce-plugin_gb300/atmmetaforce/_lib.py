@@ -126,6 +126,8 @@ _SIGS = {
     "atm_md_step": [_vp, C.c_int],
     "atm_md_get_state": [_vp, _dp, _dp, _dp, _dp, _dp, _dp],
     "atm_md_get_info": [_vp, C.POINTER(C.c_longlong), _ip, _ip],
+    "atm_md_set_recording": [_vp, C.c_int, C.c_int],
+    "atm_md_get_records": [_vp, C.POINTER(C.c_longlong), _dp, _dp, C.c_int, _ip],
     "atm_rf_nonbonded_noalloc": [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _dp, C.c_double, C.c_double, _vp, _vp,
                                  _vp],
 }

@@ -262,6 +262,26 @@ class ReplicaSimulation:
         results = [dict(zip(RES_KEYS, r.tolist())) for r in res] if res is not None else None
         return MDState(x, v, f, pe, ke, results, self.offsets)
 
+    def setRecording(self, interval, capacity=1024):
+        """Every `interval` steps (0: off), keep on the GPU the replicas' result
+        records and the R x R reduced-energy matrix at beta = 1/kT, in a ring of
+        `capacity` records (no host synchronisation per step)."""
+        self._rec_cap = int(capacity) if interval else 0
+        call("atm_md_set_recording", self._h, int(interval), int(capacity))
+
+    def getRecords(self):
+        """The kept records, oldest first, and empties the ring: steps (n,),
+        results (n, R, NUM_RES; columns in RES_KEYS order), matrices (n, R, R)."""
+        cap = getattr(self, "_rec_cap", 0)
+        steps = np.zeros(cap, dtype=np.int64)
+        res = np.zeros((cap, self.R, NUM_RES))
+        mat = np.zeros((cap, self.R, self.R))
+        n = C.c_int()
+        call("atm_md_get_records", self._h, steps.ctypes.data_as(C.POINTER(C.c_longlong)), _ptr(res), _ptr(mat),
+             cap, C.byref(n))
+        k = n.value
+        return {"steps": steps[:k], "results": res[:k], "matrices": mat[:k]}
+
     def info(self):
         steps, reorders = C.c_longlong(), C.c_int()
         dof = (C.c_int * self.R)()

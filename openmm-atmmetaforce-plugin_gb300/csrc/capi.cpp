@@ -958,6 +958,21 @@ int atm_md_get_state(atm_md_t md, double* pos, double* vel, double* forces, doub
     API_END
 }
 
+int atm_md_set_recording(atm_md_t md, int interval, int capacity) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");
+    md->md->set_recording(interval, capacity);
+    API_END
+}
+
+int atm_md_get_records(atm_md_t md, long long* steps, double* results, double* matrices, int max_records,
+                       int* n_records) {
+    API_BEGIN
+    REQUIRE(md && n_records && max_records >= 0, ATM_ERR_INVALID_ARGUMENT, "bad argument");
+    *n_records = md->md->get_records(steps, results, matrices, max_records);
+    API_END
+}
+
 int atm_md_get_info(atm_md_t md, long long* steps, int* reorders, int* dof) {
     API_BEGIN
     REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null argument");

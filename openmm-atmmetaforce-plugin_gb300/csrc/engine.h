@@ -72,6 +72,7 @@ public:
     void run_device(const double* d_pos, cudaStream_t stream);
     const double* forces_device() const { return A_.f_out; }
     const double* results_device() const { return A_.results; }
+    const double* matrix_device() const { return A_.matrix; }
     const double* box(int r) const { return specs_[r].box; }
     // Re-sort from device positions at the next evaluation (the layout, tile
     // rows and exclusion masks are rebuilt; results do not change).

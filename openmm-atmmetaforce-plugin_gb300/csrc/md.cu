@@ -495,10 +495,13 @@ MDDriver::MDDriver(const std::vector<const System*>& systems, int device, bool f
     MD_CHECK(cudaSetDevice(dev_));
     MD_CHECK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
     upload_terms(systems);
+    update_beta();
 }
 
 MDDriver::~MDDriver() {
     cudaSetDevice(dev_);
+    if (rec_res_) cudaFree(rec_res_);
+    if (rec_mat_) cudaFree(rec_mat_);
     for (void* p : allocs_) cudaFree(p);
     if (s_) cudaStreamDestroy(s_);
 }
@@ -765,6 +768,63 @@ void MDDriver::set_integrator(double T, double friction, double dt) {
     opt_.temperature = T;
     opt_.friction = friction;
     opt_.step_size = dt;
+    update_beta();
+}
+
+void MDDriver::update_beta() {
+    // the reduced-energy matrix at the integrator's temperature (beta = 1 at T = 0)
+    eng_->set_beta(opt_.temperature > 0.0 ? 1.0 / (kBoltz * opt_.temperature) : 1.0);
+    forces_valid_ = false;
+}
+
+void MDDriver::set_recording(int interval, int capacity) {
+    if (interval < 0 || (interval > 0 && capacity < 1)) throw Error(1, "Invalid recording interval or capacity");
+    MD_CHECK(cudaSetDevice(dev_));
+    if (rec_res_) cudaFree(rec_res_);
+    if (rec_mat_) cudaFree(rec_mat_);
+    rec_res_ = rec_mat_ = nullptr;
+    rec_interval_ = interval;
+    rec_cap_ = interval > 0 ? capacity : 0;
+    rec_count_ = 0;
+    rec_last_step_ = -1;
+    rec_steps_.assign(rec_cap_, 0);
+    if (rec_cap_ > 0) {
+        MD_CHECK(cudaMalloc(&rec_res_, sizeof(double) * (size_t)rec_cap_ * R_ * NUM_RES));
+        MD_CHECK(cudaMalloc(&rec_mat_, sizeof(double) * (size_t)rec_cap_ * R_ * R_));
+    }
+}
+
+// Device-to-device copies of the current evaluation into the ring (no host wait).
+void MDDriver::record_step() {
+    if (rec_interval_ <= 0 || step_ % rec_interval_ != 0 || step_ == rec_last_step_) return;
+    const int slot = (int)(rec_count_ % rec_cap_);
+    MD_CHECK(cudaMemcpyAsync(rec_res_ + (size_t)slot * R_ * NUM_RES, eng_->results_device(),
+                             sizeof(double) * R_ * NUM_RES, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaMemcpyAsync(rec_mat_ + (size_t)slot * R_ * R_, eng_->matrix_device(), sizeof(double) * R_ * R_,
+                             cudaMemcpyDeviceToDevice, s_));
+    rec_steps_[slot] = step_;
+    rec_count_++;
+    rec_last_step_ = step_;
+}
+
+int MDDriver::get_records(long long* steps, double* results, double* matrices, int max) {
+    MD_CHECK(cudaSetDevice(dev_));
+    MD_CHECK(cudaStreamSynchronize(s_));
+    const long long kept = std::min<long long>(rec_count_, rec_cap_);
+    const int n = (int)std::min<long long>(kept, std::max(0, max));
+    const long long first = rec_count_ - kept;  // oldest kept record
+    for (int k = 0; k < n; k++) {
+        const int slot = (int)((first + k) % rec_cap_);
+        if (steps) steps[k] = rec_steps_[slot];
+        if (results)
+            MD_CHECK(cudaMemcpy(results + (size_t)k * R_ * NUM_RES, rec_res_ + (size_t)slot * R_ * NUM_RES,
+                                sizeof(double) * R_ * NUM_RES, cudaMemcpyDeviceToHost));
+        if (matrices)
+            MD_CHECK(cudaMemcpy(matrices + (size_t)k * R_ * R_, rec_mat_ + (size_t)slot * R_ * R_,
+                                sizeof(double) * R_ * R_, cudaMemcpyDeviceToHost));
+    }
+    rec_count_ = 0;
+    return n;
 }
 
 void MDDriver::compute_forces() {
@@ -800,6 +860,7 @@ void MDDriver::step(int nsteps) {
     MD_CHECK(cudaSetDevice(dev_));
     for (int k = 0; k < nsteps; k++) {
         if (!forces_valid_) compute_forces();
+        record_step();
         MdDev a = dev_args();
         int nb = (n_ + 255) / 256;
         k_md_integrate<<<nb, 256, 0, s_>>>(a);

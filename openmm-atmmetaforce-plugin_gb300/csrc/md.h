@@ -94,6 +94,13 @@ public:
     // results of the ATM evaluation at the current positions
     void get_state(double* pos, double* vel, double* forces, double* potential, double* kinetic, double* results);
     int reorders() const { return reorders_; }
+    // Records of the ATM results (R x NUM_RES) and the R x R reduced-energy matrix
+    // (beta = 1/kT of the integrator) every `interval` steps, at the positions the
+    // step starts from, kept on the device in a ring of `capacity` records
+    // (interval 0: off).  get_records copies the kept records, oldest first, and
+    // empties the ring; outputs nullable, each sized for `max` records.
+    void set_recording(int interval, int capacity);
+    int get_records(long long* steps, double* results, double* matrices, int max);
     int constraint_groups() const { return n_cons_; }
     int settle_waters() const { return n_settle_; }
 
@@ -136,6 +143,14 @@ private:
     double* ke_d_ = nullptr;   // R
     int n_bonds_ = 0, n_angles_ = 0, n_posres_ = 0, n_cent_ = 0, n_cons_ = 0, n_settle_ = 0;
     std::vector<int> term_rep_;  // replica of each term, in e_terms_ order
+    // recording
+    int rec_interval_ = 0, rec_cap_ = 0;
+    long long rec_count_ = 0, rec_last_step_ = -1;
+    std::vector<long long> rec_steps_;  // ring of step numbers
+    double* rec_res_ = nullptr;         // rec_cap_ x R x NUM_RES
+    double* rec_mat_ = nullptr;         // rec_cap_ x R x R
+    void record_step();
+    void update_beta();
 };
 
 }  // namespace atm

@@ -242,3 +242,35 @@ def test_errors_are_reported():
     with pytest.raises(atm.ATMError) as e:
         atm.Simulation(sys2, atm.LangevinIntegrator(300.0, 1.0, 0.002), 0)
     assert e.value.code == 5
+
+
+def test_recording_streams_results_and_energy_matrices():
+    cases = [_case(seed=s) for s in (19, 20)]
+    cases[1][0].params = S.default_params(0.2, 0.4, 0.1, 25.0, 0.0, 200.0, 100.0, 0.0625, 1.0)
+    systems = [atm.md_system_from_case(c, t)[0] for c, t in cases]
+    integ = atm.LangevinIntegrator(300.0, 1.0, 0.002)
+    integ.setRandomNumberSeed(5)
+    rs = atm.ReplicaSimulation(systems, integ, 0)
+    rs.setPositions(np.concatenate([c.pos for c, _ in cases]))
+    rs.setVelocitiesToTemperature(300.0, 3)
+    rs.setRecording(2, capacity=8)
+    s0 = rs.getState(getEnergy=True)
+    rs.step(6)
+    rec = rs.getRecords()
+    assert list(rec["steps"]) == [0, 2, 4]
+    # the first record is the evaluation the state at step 0 reported
+    res0 = np.array([[r[k] for k in atm.RES_KEYS] for r in s0.getResults()])
+    np.testing.assert_array_equal(rec["results"][0], res0)
+    beta = 1.0 / (M.KB * 300.0)
+    iE1, iE2 = atm.RES_KEYS.index("E1"), atm.RES_KEYS.index("E2")
+    for k in range(3):
+        R = rec["results"][k]
+        for r in range(2):
+            for q in range(2):
+                ref = beta * O.atm_merge(R[r, iE1], R[r, iE2], cases[q][0].params)["energy"]
+                assert abs(rec["matrices"][k][r, q] - ref) <= 1e-9 * max(1.0, abs(ref))
+    assert len(rs.getRecords()["steps"]) == 0  # the ring was emptied
+    # a full ring keeps the newest records
+    rs.setRecording(1, capacity=2)
+    rs.step(5)
+    assert list(rs.getRecords()["steps"]) == [9, 10]
