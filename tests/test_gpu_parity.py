@@ -1,6 +1,6 @@
 """Parity of the CUDA path with the FP64 oracle, through the C ABI.
 
-Tolerances (BASELINE the benchmark spec): perturbation energy u within 0.01 kJ/mol,
+Tolerances (the targets of the path): perturbation energy u within 0.01 kJ/mol,
 force RMS relative error <= 1e-4.  Total energies, which the reference gives in
 double precision, are compared with a relative tolerance of 2e-6 of the sum of
 the magnitudes of the energy terms (FP32 pair arithmetic).
