@@ -399,8 +399,11 @@ def main():
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         threads = os.cpu_count() or 1
         v, dt = cpu_baseline(cases[0], threads, evals=2)
+        v1, dt1 = cpu_baseline(cases[0], 1, evals=1)
         cpu = {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
-               "sample": "2 evaluations of one 23,558-atom replica (two full FP64 inner evaluations + merge)"}
+               "sample": "2 evaluations of one 23,558-atom replica (two full FP64 inner evaluations + merge)",
+               "single_thread": {"value": v1, "unit": "evals/s", "cores": 1,
+                                 "sample": "1 evaluation, one thread (the serial Reference-platform shape)"}}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
