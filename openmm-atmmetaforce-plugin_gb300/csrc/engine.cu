@@ -636,6 +636,7 @@ void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream) {
     tune_brick_ = brick;
     tune_pme_stream_ = pme_stream;
     tile_grid_ = sms_ * std::min(std::max(1, tile_per_sm), max_tile_per_sm_);
+    A_.tile_dynamic = tile_dynamic();
     if (rebuild && layout_ready_ && method_ == NonbondedForce::PME) {
         build_bricks();
         alloc_device();
@@ -757,6 +758,7 @@ void Engine::alloc_device() {
     a.full = full_ ? 1 : 0;
     a.method = method_;
     a.rc2 = (float)(cutoff_ * cutoff_);
+    a.tile_dynamic = tile_dynamic();
     a.alpha = (float)alpha_;
     a.krf = (float)krf_;
     a.crf = (float)crf_;
@@ -875,6 +877,13 @@ void Engine::update_rep_table() {
 // ---------------------------------------------------------------------------
 // One evaluation: the kernel sequence (captured once into a CUDA graph)
 // ---------------------------------------------------------------------------
+
+// Hand the pair tiles out from a counter when the warps of the tile kernel get
+// many tiles each (about 15 tiles per row); a few per warp go in a fixed stride.
+int Engine::tile_dynamic() const {
+    const long long warps = (long long)tile_grid_ * (kTileThreads / 32);
+    return (long long)nrows_ * 15 >= 16 * warps ? 1 : 0;
+}
 
 int Engine::launches_per_eval() const {
     // prepare, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)

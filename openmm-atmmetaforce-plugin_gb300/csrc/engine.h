@@ -97,6 +97,7 @@ public:
     void set_profiling(bool on) { profiling_ = on; }
     const std::vector<KernelTime>& kernel_times() const { return times_; }
     int launches_per_eval() const;
+    int tile_dynamic() const;
     // tiles of the last evaluation, tile rows, and the largest row
     void stats(int* tiles, int* rows, int* max_row) const {
         if (tiles) *tiles = last_tiles_;

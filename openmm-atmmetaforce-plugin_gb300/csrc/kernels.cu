@@ -825,13 +825,14 @@ __global__ void __launch_bounds__(128, 5) k_gather(Args a) {
     Stencil S;
     make_stencil(p.x, p.y, p.z, R, S, true);
     if (a.full) {
-        float gx, gy, gz;
-        gather_one(phi1, R, S, gx, gy, gz);
-        add_grad_force(a.F, a.NA, s, p.w, gx, gy, gz, R);
+        const bool vec = ((R.real_off | (long long)R.K[2]) & 3) == 0;
+        float g[3];
+        if (!(vec && gather_vec<1>(phi1, nullptr, R, S, g, nullptr, nullptr))) gather_one(phi1, R, S, g[0], g[1], g[2]);
+        add_grad_force(a.F, a.NA, s, p.w, g[0], g[1], g[2], R);
         const float4 p2 = a.posq2[s];
         make_stencil(p2.x, p2.y, p2.z, R, S, true);
-        gather_one(phi2, R, S, gx, gy, gz);
-        add_grad_force(F2, a.NA, s, p.w, gx, gy, gz, R);
+        if (!(vec && gather_vec<1>(phi2, nullptr, R, S, g, nullptr, nullptr))) gather_one(phi2, R, S, g[0], g[1], g[2]);
+        add_grad_force(F2, a.NA, s, p.w, g[0], g[1], g[2], R);
     } else {
         // F1 from the state-1 potential; F2 - F1 from the potential of the moved charges
         float g1[3], g2[3], pot2 = 0.f;
@@ -937,18 +938,6 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
     out[RES_DWDU] = (alpha > 0 ? bfp : l2) * fp;
 }
 
-__device__ double block_sum(double v, double* sh) {
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    double r = sh[0];
-    __syncthreads();
-    return r;
-}
-
 // Energy of each tile row, one warp per row (lanes over the row's slots, fixed order).
 __global__ void k_rowsum(Args a) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -969,27 +958,35 @@ __device__ double rows_sum(const Args& a, int rb, int re) {
 }
 
 __global__ void __launch_bounds__(256) k_finalize(Args a) {
-    __shared__ double sh[256];
-    int r = blockIdx.x;
+    // seven sums per replica in one fixed-order reduction: direct-space rows of
+    // state 1 and state 2 / difference, exceptions (3), reciprocal (2)
+    __shared__ double sh[7][8];
+    const int r = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const RepDev& R = a.reps[r];
-    double dir1 = block_sum(rows_sum(a, R.row1_b, R.row1_e), sh);
-    double dir2 = block_sum(rows_sum(a, R.row2_b, R.row2_e), sh);
-    double x1 = 0, x2 = 0, xd = 0, c1 = 0, c2 = 0;
+    double v[7] = {rows_sum(a, R.row1_b, R.row1_e), rows_sum(a, R.row2_b, R.row2_e), 0, 0, 0, 0, 0};
     for (int c = R.exc_cta_b + threadIdx.x; c < R.exc_cta_e; c += blockDim.x) {
-        x1 += a.e_part_exc[3 * c];
-        x2 += a.e_part_exc[3 * c + 1];
-        xd += a.e_part_exc[3 * c + 2];
+        v[2] += a.e_part_exc[3 * c];
+        v[3] += a.e_part_exc[3 * c + 1];
+        v[4] += a.e_part_exc[3 * c + 2];
     }
     for (int c = R.conv_cta_b + threadIdx.x; c < R.conv_cta_e; c += blockDim.x) {
-        c1 += a.e_part_conv[2 * c];
-        c2 += a.e_part_conv[2 * c + 1];
+        v[5] += a.e_part_conv[2 * c];
+        v[6] += a.e_part_conv[2 * c + 1];
     }
-    x1 = block_sum(x1, sh);
-    x2 = block_sum(x2, sh);
-    xd = block_sum(xd, sh);
-    c1 = block_sum(c1, sh);
-    c2 = block_sum(c2, sh);
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], o);
+        if (lane == 0) sh[k][w] = v[k];
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
+        double t[7];
+        for (int k = 0; k < 7; k++) {
+            t[k] = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); q++) t[k] += sh[k][q];
+        }
+        const double dir1 = t[0], dir2 = t[1], x1 = t[2], x2 = t[3], xd = t[4], c1 = t[5], c2 = t[6];
         double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
         double E2;
         if (a.full) {

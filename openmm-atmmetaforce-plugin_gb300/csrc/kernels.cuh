@@ -114,6 +114,7 @@ struct Args {
     const int2* dx_ent;
     const uint32_t* masks;    // 32 words per mask
     int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
+    int tile_dynamic;         // 1: pair tiles handed out from a counter (large lists)
     int* tile_j;              // 32 j slots per tile (atom tiles)
     double* e_tile;           // nrows*row_cap
     double* e_row;            // nrows: sum of each row's tiles

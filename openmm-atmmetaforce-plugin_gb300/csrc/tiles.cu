@@ -286,11 +286,12 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
     __shared__ int s_stage[kFindWarps][kStageAtoms];
     __shared__ float4 s_ipos[kFindWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int mine = 0;
-    if (lane == 0) mine = atomicAdd(&a.status->next_row, 1);
-    int k = __shfl_sync(FULL_MASK, mine, 0);
+    // the first row of every warp is fixed, the later ones come from the counter
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int mine = a.nrows;
     while (k < a.nrows) {
-        if (lane == 0) mine = atomicAdd(&a.status->next_row, 1);
+        if (lane == 0) mine = nw < a.nrows ? nw + atomicAdd(&a.status->next_row, 1) : a.nrows;
         find_row(a, a.nrows - 1 - k, lane, s_stage[w], s_ipos[w]);
         __syncwarp();
         k = __shfl_sync(FULL_MASK, mine, 0);
@@ -445,7 +446,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
     }
 }
 
-template <int METHOD>
+template <int METHOD, bool DYN>
 __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     __shared__ float4 s_p[kTileThreads / 32][64];
     __shared__ float2 s_l[kTileThreads / 32][64];
@@ -453,14 +454,16 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     int ntiles = a.status->tile_count;
     if (ntiles > a.tile_cap) ntiles = a.tile_cap;
     const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
-    // tiles are handed out kTileGrab at a time from a counter, the next grab
-    // requested before the current one is processed, so that warps finish together
+    // Large lists: tiles handed out kTileGrab at a time from a counter (the next
+    // grab requested before the current tiles are processed), so that warps finish
+    // together.  Small lists (a few tiles per warp): warp w takes tiles w, w + nw, ...
+    // (DYN, chosen by the host from the size of the row list)
     int mine = 0;
-    if (lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
-    int cur = __shfl_sync(FULL_MASK, mine, 0);
+    if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+    int cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     while (cur < ntiles) {
-    if (lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
-    const int cur_end = min(cur + kTileGrab, ntiles);
+    if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+    const int cur_end = DYN ? min(cur + kTileGrab, ntiles) : cur + 1;
     for (int t = cur; t < cur_end; t++) {
         const int4 T = a.tiles[t];
         const int I = T.x;
@@ -594,22 +597,29 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
             }
         }
     }
-    cur = __shfl_sync(FULL_MASK, mine, 0);
+    cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : cur + ((gridDim.x * blockDim.x) >> 5);
     }
 }
 
 int tiles_kernel_blocks_per_sm() {
     int n4 = 0, n2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4>, kTileThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4, true>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2, true>, kTileThreads, 0);
     return n4 < n2 ? n4 : n2;
 }
 
 void launch_tiles(const Args& a, int grid, cudaStream_t s) {
-    if (a.method == 4)
-        k_tiles<4><<<grid, kTileThreads, 0, s>>>(a);
-    else
-        k_tiles<2><<<grid, kTileThreads, 0, s>>>(a);
+    if (a.method == 4) {
+        if (a.tile_dynamic)
+            k_tiles<4, true><<<grid, kTileThreads, 0, s>>>(a);
+        else
+            k_tiles<4, false><<<grid, kTileThreads, 0, s>>>(a);
+    } else {
+        if (a.tile_dynamic)
+            k_tiles<2, true><<<grid, kTileThreads, 0, s>>>(a);
+        else
+            k_tiles<2, false><<<grid, kTileThreads, 0, s>>>(a);
+    }
 }
 
 }  // namespace atm
