@@ -26,9 +26,8 @@ namespace atm {
 #define FULL_MASK 0xffffffffu
 
 __device__ __forceinline__ void fix_add(unsigned long long* p, float v) {
-    // cvt.rni.s64.f32 saturates out-of-range values; the sum of two's-complement
-    // integers is exact and order independent
-    atomicAdd(p, (unsigned long long)__float2ll_rn(v * kFixScaleF));
+    // the sum of two's-complement integers is exact and order independent
+    atomicAdd(p, fix_bits(v));
 }
 
 __device__ __forceinline__ void fix_add_d(unsigned long long* p, double v) {

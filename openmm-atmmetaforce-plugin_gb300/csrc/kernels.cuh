@@ -15,8 +15,21 @@ namespace atm {
 
 constexpr int kTile = 32;
 constexpr double kFixScale = 4294967296.0;  // 2^32
-constexpr float kFixScaleF = 4294967296.0f;
 constexpr int kOrder = 5;  // PME B-spline order (OpenMM's)
+
+// round(v * 2^32) as a 64-bit two's-complement integer, from 32-bit conversions
+// only (64-bit conversions issue on the FP64 pipe, which is narrow on this GPU).
+// With h = floor(v), f = v - h is exact and lies in [0, 1), so
+// round(v 2^32) = h 2^32 + round(f 2^32), and f 2^32 <= 2^32 - 2^8 never rounds up
+// to 2^32.  Equal to cvt.rni.s64.f32 of v 2^32 for |v| < 2^31 (both saturate beyond).
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned long long fix_bits(float v) {
+    const float h = floorf(v);
+    const unsigned lo = __float2uint_rn((v - h) * 4294967296.0f);
+    const unsigned hi = (unsigned)__float2int_rz(h);
+    return ((unsigned long long)hi << 32) | lo;
+}
+#endif
 
 // Row kinds of the pair-tile lists.
 enum RowKind { ROW_STATE1 = 0, ROW_STATE2 = 1, ROW_DIFF1 = 2, ROW_DIFF2 = 3 };

@@ -32,7 +32,7 @@ constexpr int kFindWarps = 4;
 constexpr int kTileGrab = 4;  // tiles per grab of the pair-tile kernel
 
 __device__ __forceinline__ void fix_add_t(unsigned long long* p, float v) {
-    atomicAdd(p, (unsigned long long)__float2ll_rn(v * kFixScaleF));
+    atomicAdd(p, fix_bits(v));
 }
 
 __device__ __forceinline__ float min_img(float d, float L, float iL) { return d - L * rintf(d * iL); }
@@ -68,14 +68,90 @@ __device__ __forceinline__ void row_box(const Args& a, int I, int kind, float4& 
     }
 }
 
+constexpr int kStageAtoms = 2048;  // culled atoms staged in shared memory per row
+
+// Position of slot s at the geometry of a row kind, as the pair-tile kernel reads it.
+__device__ __forceinline__ float4 row_pos(const Args& a, int kind, int s) {
+    float4 p = (kind == ROW_STATE2 ? a.posq2 : a.posq)[s];
+    if (kind == ROW_DIFF2) {
+        const float4 d = a.displ[s];
+        p.x += d.x;
+        p.y += d.y;
+        p.z += d.z;
+    }
+    return p;
+}
+
+// Positions of the atoms of block I at the geometry of a row, taken to the
+// periodic image nearest the box centre (as the pair-tile kernel does), into the
+// warp's shared memory for the exact cut.
+__device__ __forceinline__ void load_ipos(const Args& a, const RepDev& R, int I, int kind, float4 ci, int lane,
+                                          float4* s_ipos) {
+    float4 pi = row_pos(a, kind, I * kTile + lane);
+    pi.x = ci.x + min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
+    pi.y = ci.y + min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
+    pi.z = ci.z + min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
+    s_ipos[lane] = pi;
+    __syncwarp();
+}
+
+// Second cut of staged atoms list[from, natom): keeps the atoms j within the
+// cutoff of at least one atom of block I (the box test keeps every atom within
+// the cutoff of the box, corners included).  Positions are taken to the periodic
+// image nearest the box centre, as the pair-tile kernel does; the threshold is
+// widened by 1e-5 so that no pair the kernel counts can be dropped by rounding.
+// In place, order kept; returns from + the number kept.
+__device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
+                                         int from, int natom, const float4* s_ipos) {
+    const float rc2 = a.rc2 * 1.00001f;
+    int kept = from;
+    for (int g = from; g < natom; g += 32) {
+        const int k = g + lane;
+        const bool valid = k < natom;
+        const int j = valid ? list[k] : 0;
+        bool hit = false;
+        float4 p = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);  // invalid lanes never hit
+        if (valid) {
+            p = row_pos(a, kind, j);
+            p.x = ci.x + min_img(p.x - ci.x, R.box[0], R.ibox[0]);
+            p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
+            p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
+        }
+        // eight i atoms at a time; stop once every lane has decided
+        for (int q0 = 0; q0 < 32; q0 += 8) {
+#pragma unroll
+            for (int q = q0; q < q0 + 8; q++) {
+                const float4 o = s_ipos[q];
+                const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
+                hit |= dx * dx + dy * dy + dz * dz < rc2;
+            }
+            if (__all_sync(FULL_MASK, hit || !valid)) break;
+        }
+        __syncwarp();
+        const bool keep = valid && hit;
+        const unsigned b = __ballot_sync(FULL_MASK, keep);
+        if (keep) list[kept + __popc(b & ((1u << lane) - 1u))] = j;
+        kept += __popc(b);
+        __syncwarp();
+    }
+    return kept;
+}
+
 // One pass over the candidate blocks of a row (bounding boxes closer than the
 // cutoff, no exclusion with I) and their atoms within the cutoff of block I's
-// box.  Counts the atoms; with out != nullptr also writes the first cap of them,
-// in a fixed order, to consecutive j slots.  The row's exclusion partners are
-// held one per lane (rows with more than 32 fall back to reading the list), and
-// four candidate blocks are loaded per step so that their latencies overlap.
+// box, written in a fixed order to consecutive j slots of out.
+//   CUT = false: returns the number of atoms and writes the first cap of them.
+//   CUT = true (out: the warp's stage in shared memory, s_ipos loaded): whenever
+//     the stage nears cap, the exact cut thins the atoms staged since the last
+//     cut; returns the number of atoms kept, or -1 when they do not fit (then
+//     raw holds the number of atoms before any cut).
+// The row's exclusion partners are held one per lane (rows with more than 32 fall
+// back to reading the list), and four candidate blocks are loaded per step so
+// that their latencies overlap.
+template <bool CUT>
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
-                                         const int2* ee, int e0, int e1, int lane, int* out, int cap) {
+                                         const int2* ee, int e0, int e1, int lane, int* out, int cap,
+                                         const float4* s_ipos, int& raw) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
@@ -83,7 +159,9 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
     const float4* BH = kind == ROW_STATE2 ? a.bb_h2 : a.bb_h;
     const int nex = e1 - e0;
     const int my_ex = lane < nex ? ee[e0 + lane].x : -1;
-    int natom = 0;
+    int natom = 0, cut_from = 0;
+    bool over = false;
+    raw = 0;
     const int jb = diff ? R.block_begin : I + 1;
     for (int base = jb; base < R.block_end; base += 32) {
         const int Jl = base + lane;
@@ -147,76 +225,25 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             for (int t = 0; t < 4; t++) {
                 const bool in = lane < n[t] && point_close(ci, hi, p[t], R, a.rc2);
                 const unsigned b = __ballot_sync(FULL_MASK, in);
-                if (out) {
-                    const int k = natom + __popc(b & ((1u << lane) - 1u));
-                    if (in && k < cap) out[k] = J[t] * kTile + lane;
-                }
+                const int k = natom + __popc(b & ((1u << lane) - 1u));
+                if (in && k < cap && !over) out[k] = J[t] * kTile + lane;
                 natom += __popc(b);
+                raw += __popc(b);
+            }
+            if (CUT && !over && natom > cap - 4 * kTile) {
+                __syncwarp();
+                natom = exact_cut(a, R, kind, ci, lane, out, cut_from, min(natom, cap), s_ipos);
+                cut_from = natom;
+                over = natom > cap - 4 * kTile;
             }
         }
+    }
+    if (CUT) {
+        if (over) return -1;
+        __syncwarp();
+        natom = exact_cut(a, R, kind, ci, lane, out, cut_from, natom, s_ipos);
     }
     return natom;
-}
-
-constexpr int kStageAtoms = 1024;  // culled atoms staged in shared memory per row
-
-// Position of slot s at the geometry of a row kind, as the pair-tile kernel reads it.
-__device__ __forceinline__ float4 row_pos(const Args& a, int kind, int s) {
-    float4 p = (kind == ROW_STATE2 ? a.posq2 : a.posq)[s];
-    if (kind == ROW_DIFF2) {
-        const float4 d = a.displ[s];
-        p.x += d.x;
-        p.y += d.y;
-        p.z += d.z;
-    }
-    return p;
-}
-
-// Second cut of a staged row: keeps the atoms j within the cutoff of at least one
-// atom of block I (the box test keeps every atom within the cutoff of the box,
-// corners included).  Positions are taken to the periodic image nearest the
-// box centre, as the pair-tile kernel does; the threshold is widened by 1e-5 so
-// that no pair the kernel counts can be dropped by rounding.  In place, order kept.
-__device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int I, int kind, float4 ci, int lane,
-                                         int* list, int natom, float4* s_ipos) {
-    float4 pi = row_pos(a, kind, I * kTile + lane);
-    pi.x = ci.x + min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
-    pi.y = ci.y + min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
-    pi.z = ci.z + min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
-    s_ipos[lane] = pi;
-    __syncwarp();
-    const float rc2 = a.rc2 * 1.00001f;
-    int kept = 0;
-    for (int g = 0; g < natom; g += 32) {
-        const int k = g + lane;
-        const bool valid = k < natom;
-        const int j = valid ? list[k] : 0;
-        bool hit = false;
-        float4 p = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);  // invalid lanes never hit
-        if (valid) {
-            p = row_pos(a, kind, j);
-            p.x = ci.x + min_img(p.x - ci.x, R.box[0], R.ibox[0]);
-            p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
-            p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
-        }
-        // eight i atoms at a time; stop once every lane has decided
-        for (int q0 = 0; q0 < 32; q0 += 8) {
-#pragma unroll
-            for (int q = q0; q < q0 + 8; q++) {
-                const float4 o = s_ipos[q];
-                const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
-                hit |= dx * dx + dy * dy + dz * dz < rc2;
-            }
-            if (__all_sync(FULL_MASK, hit || !valid)) break;
-        }
-        __syncwarp();
-        const bool keep = valid && hit;
-        const unsigned b = __ballot_sync(FULL_MASK, keep);
-        if (keep) list[kept + __popc(b & ((1u << lane) - 1u))] = j;
-        kept += __popc(b);
-        __syncwarp();
-    }
-    return kept;
 }
 
 // The tiles of one row (one warp; stage and ipos: the warp's shared memory).
@@ -237,10 +264,19 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
                           rc + 2.f * hi.z >= 0.5f * R.box[2])
                              ? 1u
                              : 0u;
-    // staged in shared memory; rows longer than the stage are written by a second pass
-    int natom = row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms);
+    // staged in shared memory and cut there; rows whose atoms do not fit, and rows
+    // that need per-pair images (no exact cut), are written by a second pass
+    int raw = 0, natom = -1;
+    if (!pbc) {
+        load_ipos(a, R, I, kind, ci, lane, ipos);
+        natom = row_atoms<true>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw);
+    } else {
+        natom = row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw);
+        if (natom > kStageAtoms) natom = -1;
+    }
     __syncwarp();
-    if (natom <= kStageAtoms && !pbc) natom = exact_cut(a, R, I, kind, ci, lane, stage, natom, ipos);
+    const bool staged = natom >= 0;
+    if (!staged) natom = raw;
     const int nblock = e1 - e0;
     const int natile = (natom + 31) / 32;
     int n = nblock + natile;
@@ -259,11 +295,11 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
         return;
     }
     int* out = a.tile_j + (size_t)(tbase + nblock) * 32;
-    if (natom <= kStageAtoms) {
+    if (staged) {
         for (int k = lane; k < natom; k += 32) out[k] = stage[k];
     } else {
         // second pass: the same atoms, in the same order, straight into the j slots
-        row_atoms(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom);
+        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom, ipos, raw);
     }
     for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
     const int zword = row | (kind << 28);
