@@ -682,7 +682,7 @@ std::string Engine::autotune(int trials, bool use_cache) {
     int bt = max_tile_per_sm_, bb = tune_brick_;
     bool bs = tune_pme_stream_;
     const bool pme = method_ == NonbondedForce::PME;
-    std::vector<int> bricks = pme ? std::vector<int>{16, 12, 8} : std::vector<int>{tune_brick_};
+    std::vector<int> bricks = pme ? std::vector<int>{20, 16, 12, 8} : std::vector<int>{tune_brick_};
     std::vector<int> pmes = pme ? std::vector<int>{1, 0} : std::vector<int>{1};
     cudaEvent_t e0, e1;
     CUDA_CHECK(cudaEventCreate(&e0));
