@@ -888,12 +888,7 @@ int Engine::tile_dynamic() const {
 int Engine::launches_per_eval() const {
     // prepare, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)
     int n = 4 + 4;
-    if (method_ == NonbondedForce::PME) n += 3;  // spread, conv, gather
-    if (method_ == NonbondedForce::PME && !full_) {
-        bool any = false;
-        for (int c : block_cls_) any |= c != 0;
-        n += any ? 1 : 0;  // gather of the moving atoms
-    }
+    if (method_ == NonbondedForce::PME) n += 3;  // spread, conv, gather (moving atoms included)
     return n;
 }
 
@@ -919,6 +914,9 @@ void Engine::record(cudaStream_t st, bool host_io) {
             CUFFT_CHECK(cufftSetStream(g.fwd, ps));
             CUFFT_CHECK(cufftSetStream(g.inv, ps));
         }
+        // the exceptions need neither lists nor grids: they go first on this
+        // stream, beside the list building
+        launch_exceptions(a, ps);
         launch_spread(a, ps);
         for (auto& g : groups_)
             CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
@@ -930,7 +928,7 @@ void Engine::record(cudaStream_t st, bool host_io) {
     }
     launch_find(a, st);
     launch_tiles(a, tile_grid_, st);
-    launch_exceptions(a, st);
+    if (!pme) launch_exceptions(a, st);
     if (pme && tune_pme_stream_) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
     launch_finalize(a, st);
     launch_output(a, st);

@@ -685,63 +685,18 @@ __device__ __forceinline__ void gather_one(const float* G, const RepDev& R, cons
     if (pot) *pot = ph;
 }
 
-// Gradients of two grids at one stencil (the state-1 potential and the
-// potential of the moved charges).
-__device__ __forceinline__ void gather_two(const float* G1, const float* G2, const RepDev& R, const Stencil& S,
-                                           float* g1, float* g2, float* pot2 = nullptr) {
-    float ph2 = 0.f;
-    const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
-    int iz[5];
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        int v = S.base[2] - c;
-        iz[c] = v < 0 ? v + Kz : v;
-    }
-    g1[0] = g1[1] = g1[2] = g2[0] = g2[1] = g2[2] = 0.f;
-#pragma unroll
-    for (int a0 = 0; a0 < 5; a0++) {
-        int ix = S.base[0] - a0;
-        if (ix < 0) ix += Kx;
-#pragma unroll
-        for (int b0 = 0; b0 < 5; b0++) {
-            int iy = S.base[1] - b0;
-            if (iy < 0) iy += Ky;
-            const size_t rowo = ((size_t)ix * Ky + iy) * Kz;
-            float s1 = 0.f, z1 = 0.f, s2 = 0.f, z2 = 0.f;
-#pragma unroll
-            for (int c0 = 0; c0 < 5; c0++) {
-                const float v1 = __ldg(G1 + rowo + iz[c0]);
-                const float v2 = __ldg(G2 + rowo + iz[c0]);
-                s1 += S.w[2][c0] * v1;
-                z1 += S.dw[2][c0] * v1;
-                s2 += S.w[2][c0] * v2;
-                z2 += S.dw[2][c0] * v2;
-            }
-            const float dxy = S.dw[0][a0] * S.w[1][b0], xdy = S.w[0][a0] * S.dw[1][b0], xy = S.w[0][a0] * S.w[1][b0];
-            g1[0] += dxy * s1;
-            g1[1] += xdy * s1;
-            g1[2] += xy * z1;
-            g2[0] += dxy * s2;
-            g2[1] += xdy * s2;
-            g2[2] += xy * z2;
-            if (pot2) ph2 += xy * s2;
-        }
-    }
-    if (pot2) *pot2 = ph2;
-}
-
 __device__ __forceinline__ float pick5(const float* w, int k) {
     return k == 0 ? w[0] : k == 1 ? w[1] : k == 2 ? w[2] : k == 3 ? w[3] : k == 4 ? w[4] : 0.0f;
 }
 
-// Gradients of NG grids at one stencil with 16-byte loads: the five z points
-// base - 4 .. base of every (x, y) row lie in the aligned eight-float window that
-// starts at az = (base - 4) & ~3, read as two float4; the z weights are re-indexed
-// into that window once.  Returns false (nothing computed) when the window would
-// wrap around the grid; grids must start 16-byte aligned with Kz a multiple of 4.
-template <int NG>
-__device__ __forceinline__ bool gather_vec(const float* G0, const float* G1, const RepDev& R, const Stencil& S,
-                                           float* g0, float* g1, float* pot1) {
+// Gradient of one grid at one stencil (and with POT the potential) with 16-byte
+// loads: the five z points base - 4 .. base of every (x, y) row lie in the
+// aligned eight-float window that starts at az = (base - 4) & ~3, read as two
+// float4; the z weights are re-indexed into that window once.  Returns false
+// (nothing computed) when the window would wrap around the grid; the grid must
+// start 16-byte aligned with Kz a multiple of 4.
+template <bool POT>
+__device__ __forceinline__ bool gather_vec(const float* G, const RepDev& R, const Stencil& S, float* g, float* pot) {
     const int Kx = R.K[0], Ky = R.K[1], Kz = R.K[2];
     const int z0 = S.base[2] - (kOrder - 1);
     const int az = z0 & ~3;
@@ -754,7 +709,7 @@ __device__ __forceinline__ bool gather_vec(const float* G0, const float* G1, con
         Wz[k] = pick5(S.w[2], c);
         dWz[k] = pick5(S.dw[2], c);
     }
-    float a0x = 0.f, a0y = 0.f, a0z = 0.f, a1x = 0.f, a1y = 0.f, a1z = 0.f, p1 = 0.f;
+    float ax = 0.f, ay = 0.f, az_ = 0.f, ph = 0.f;
 #pragma unroll
     for (int i0 = 0; i0 < kOrder; i0++) {
         int ix = S.base[0] - i0;
@@ -765,38 +720,21 @@ __device__ __forceinline__ bool gather_vec(const float* G0, const float* G1, con
             if (iy < 0) iy += Ky;
             const size_t ro = ((size_t)ix * Ky + iy) * Kz + az;
             const float dxy = S.dw[0][i0] * S.w[1][j0], xdy = S.w[0][i0] * S.dw[1][j0], xy = S.w[0][i0] * S.w[1][j0];
-            {
-                const float4 lo = __ldg((const float4*)(G0 + ro)), hi = __ldg((const float4*)(G0 + ro + 4));
-                const float sx = Wz[0] * lo.x + Wz[1] * lo.y + Wz[2] * lo.z + Wz[3] * lo.w + Wz[4] * hi.x +
-                                 Wz[5] * hi.y + Wz[6] * hi.z + Wz[7] * hi.w;
-                const float sz = dWz[0] * lo.x + dWz[1] * lo.y + dWz[2] * lo.z + dWz[3] * lo.w + dWz[4] * hi.x +
-                                 dWz[5] * hi.y + dWz[6] * hi.z + dWz[7] * hi.w;
-                a0x += dxy * sx;
-                a0y += xdy * sx;
-                a0z += xy * sz;
-            }
-            if (NG == 2) {
-                const float4 lo = __ldg((const float4*)(G1 + ro)), hi = __ldg((const float4*)(G1 + ro + 4));
-                const float sx = Wz[0] * lo.x + Wz[1] * lo.y + Wz[2] * lo.z + Wz[3] * lo.w + Wz[4] * hi.x +
-                                 Wz[5] * hi.y + Wz[6] * hi.z + Wz[7] * hi.w;
-                const float sz = dWz[0] * lo.x + dWz[1] * lo.y + dWz[2] * lo.z + dWz[3] * lo.w + dWz[4] * hi.x +
-                                 dWz[5] * hi.y + dWz[6] * hi.z + dWz[7] * hi.w;
-                a1x += dxy * sx;
-                a1y += xdy * sx;
-                a1z += xy * sz;
-                p1 += xy * sx;
-            }
+            const float4 lo = __ldg((const float4*)(G + ro)), hi = __ldg((const float4*)(G + ro + 4));
+            const float sx = Wz[0] * lo.x + Wz[1] * lo.y + Wz[2] * lo.z + Wz[3] * lo.w + Wz[4] * hi.x +
+                             Wz[5] * hi.y + Wz[6] * hi.z + Wz[7] * hi.w;
+            const float sz = dWz[0] * lo.x + dWz[1] * lo.y + dWz[2] * lo.z + dWz[3] * lo.w + dWz[4] * hi.x +
+                             dWz[5] * hi.y + dWz[6] * hi.z + dWz[7] * hi.w;
+            ax += dxy * sx;
+            ay += xdy * sx;
+            az_ += xy * sz;
+            if (POT) ph += xy * sx;
         }
     }
-    g0[0] = a0x;
-    g0[1] = a0y;
-    g0[2] = a0z;
-    if (NG == 2) {
-        g1[0] = a1x;
-        g1[1] = a1y;
-        g1[2] = a1z;
-        if (pot1) *pot1 = p1;
-    }
+    g[0] = ax;
+    g[1] = ay;
+    g[2] = az_;
+    if (POT) *pot = ph;
     return true;
 }
 
@@ -808,72 +746,90 @@ __device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, in
 }
 
 // Reciprocal-space forces of every atom that does not move (difference mode)
-// or of every atom at both states (two-state mode).
-__global__ void __launch_bounds__(128, 5) k_gather(Args a) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.NA) return;
-    const int b = s >> 5;
-    if (!a.full && a.block_cls[b] != 0) return;  // moving atoms: k_gather_moving
-    const RepDev& R = a.reps[a.block_rep[b]];
-    const float4 p = a.posq[s];
-    if (p.w == 0.0f) return;
-    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
-    const float* phi1 = a.qreal + R.real_off;
-    const float* phi2 = phi1 + G3;
-    unsigned long long* F2 = a.F + 3 * (size_t)a.NA;
-    Stencil S;
-    make_stencil(p.x, p.y, p.z, R, S, true);
-    if (a.full) {
-        const bool vec = ((R.real_off | (long long)R.K[2]) & 3) == 0;
-        float g[3];
-        if (!(vec && gather_vec<1>(phi1, nullptr, R, S, g, nullptr, nullptr))) gather_one(phi1, R, S, g[0], g[1], g[2]);
-        add_grad_force(a.F, a.NA, s, p.w, g[0], g[1], g[2], R);
-        const float4 p2 = a.posq2[s];
-        make_stencil(p2.x, p2.y, p2.z, R, S, true);
-        if (!(vec && gather_vec<1>(phi2, nullptr, R, S, g, nullptr, nullptr))) gather_one(phi2, R, S, g[0], g[1], g[2]);
-        add_grad_force(F2, a.NA, s, p.w, g[0], g[1], g[2], R);
+// or of every atom at both states (two-state mode).  Two threads per atom, one
+// per grid (the two halves of a CTA: 64 atoms, grid 0 then grid 1), so that each
+// thread holds one grid's sums and more warps hide the grid reads' latency.
+constexpr int kGatherAtoms = 64;
+
+// Gradient of one grid at a stencil (and with pot != nullptr its potential):
+// the aligned float4 windows where they fit, single points otherwise.
+__device__ __forceinline__ void gather_grid(const float* G, const RepDev& R, const Stencil& S, float* g, float* pot) {
+    const bool vec = ((R.real_off | (long long)R.K[2]) & 3) == 0;
+    if (pot) {
+        if (!(vec && gather_vec<true>(G, R, S, g, pot))) gather_one(G, R, S, g[0], g[1], g[2], pot);
     } else {
-        // F1 from the state-1 potential; F2 - F1 from the potential of the moved charges
-        float g1[3], g2[3], pot2 = 0.f;
-        const bool vec = ((R.real_off | (long long)R.K[2]) & 3) == 0;
-        if (!(vec && gather_vec<2>(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr)))
-            gather_two(phi1, phi2, R, S, g1, g2, a.adjoint ? &pot2 : nullptr);
-        add_grad_force(a.F, a.NA, s, p.w, g1[0], g1[1], g1[2], R);
-        add_grad_force(F2, a.NA, s, p.w, g2[0], g2[1], g2[2], R);
-        if (a.adjoint) fix_add(a.D + s, pot2);  // d(E2 - E1)_rec / d(scaled charge)
+        if (!(vec && gather_vec<false>(G, R, S, g, nullptr))) gather_one(G, R, S, g[0], g[1], g[2]);
     }
 }
 
-// Moving atoms of the difference mode: F1 at x in phi1, and F2 - F1 =
-// F(x + d in phi1 + dphi) - F(x in phi1).
-__global__ void k_gather_moving(Args a) {
-    const int blk = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (blk >= a.n_mov_blocks) return;
+// The moving atoms of the difference mode, one CTA per moving block, warps 0-2
+// on the three gathers of F1 at x in phi1 and F2 - F1 = F(x + d in phi1 + dphi)
+// - F(x in phi1):  warp 0: phi1 at x (F1 += g, F2 -= g), warp 1: phi1 at x + d,
+// warp 2: dphi at x + d (F2 += each).  Fixed-point sums: the order is immaterial.
+__device__ __noinline__ void gather_moving(const Args& a, int blk) {
+    const int w = threadIdx.x >> 5;
+    if (w > 2) return;
     const int b = a.mov_blocks[blk];
     const int s = b * kTile + (threadIdx.x & 31);
     const RepDev& R = a.reps[a.block_rep[b]];
     const float4 p = a.posq[s];
     if (p.w == 0.0f) return;
     const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
-    const float* phi1 = a.qreal + R.real_off;
-    const float* phi2 = phi1 + G3;
+    const float* G = a.qreal + R.real_off + (w == 2 ? G3 : 0);
+    Stencil S;
+    if (w == 0) {
+        make_stencil(p.x, p.y, p.z, R, S, true);
+    } else {
+        const float4 d = a.displ[s];
+        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
+                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
+    }
+    float g[3], pot = 0.f;
+    gather_grid(G, R, S, g, a.adjoint ? &pot : nullptr);
+    unsigned long long* F2 = a.F + 3 * (size_t)a.NA;
+    if (w == 0) {
+        add_grad_force(a.F, a.NA, s, p.w, g[0], g[1], g[2], R);
+        add_grad_force(F2, a.NA, s, p.w, -g[0], -g[1], -g[2], R);
+        if (a.adjoint) fix_add(a.D + s, -pot);  // potential at x + d in state 2 minus at x in state 1
+    } else {
+        add_grad_force(F2, a.NA, s, p.w, g[0], g[1], g[2], R);
+        if (a.adjoint) fix_add(a.D + s, pot);
+    }
+}
+
+__global__ void __launch_bounds__(2 * kGatherAtoms, 6) k_gather(Args a) {
+    const int nmain = (a.NA + kGatherAtoms - 1) / kGatherAtoms;
+    if ((int)blockIdx.x >= nmain) {
+        gather_moving(a, blockIdx.x - nmain);
+        return;
+    }
+    const int half = threadIdx.x / kGatherAtoms;  // warp-uniform
+    const int s = blockIdx.x * kGatherAtoms + (threadIdx.x - half * kGatherAtoms);
+    if (s >= a.NA) return;
+    const int b = s >> 5;
+    if (!a.full && a.block_cls[b] != 0) return;  // moving atoms: the CTAs after the first nmain
+    const RepDev& R = a.reps[a.block_rep[b]];
+    const float q = a.posq[s].w;
+    if (q == 0.0f) return;
+    const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
+    const float* G = a.qreal + R.real_off + (half ? G3 : 0);
+    unsigned long long* F = a.F + (half ? 3 * (size_t)a.NA : 0);
+    // two-state mode: grid 1 is state 2 at x + d; difference mode: the potential
+    // of the moved charges at x (F2 - F1 and, for the adjoint, d(E2 - E1)_rec/dq)
+    const float4 p = (a.full && half) ? a.posq2[s] : a.posq[s];
     Stencil S;
     make_stencil(p.x, p.y, p.z, R, S, true);
-    float gx, gy, gz, hx, hy, hz, kx, ky, kz, pg, ph, pk;
-    gather_one(phi1, R, S, gx, gy, gz, &pg);
-    add_grad_force(a.F, a.NA, s, p.w, gx, gy, gz, R);
-    const float4 d = a.displ[s];
-    make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
-                 wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
-    gather_one(phi1, R, S, hx, hy, hz, &ph);
-    gather_one(phi2, R, S, kx, ky, kz, &pk);
-    add_grad_force(a.F + 3 * (size_t)a.NA, a.NA, s, p.w, hx + kx - gx, hy + ky - gy, hz + kz - gz, R);
-    if (a.adjoint) fix_add(a.D + s, ph + pk - pg);  // potential at x + d in state 2 minus at x in state 1
+    float g[3], pot = 0.f;
+    const bool with_pot = !a.full && half && a.adjoint;
+    gather_grid(G, R, S, g, with_pot ? &pot : nullptr);
+    if (with_pot) fix_add(a.D + s, pot);
+    add_grad_force(F, a.NA, s, q, g[0], g[1], g[2], R);
 }
 
 void launch_gather(const Args& a, cudaStream_t s) {
-    k_gather<<<(a.NA + 127) / 128, 128, 0, s>>>(a);
-    if (!a.full && a.n_mov_blocks > 0) k_gather_moving<<<(a.n_mov_blocks + 3) / 4, 128, 0, s>>>(a);
+    const int nmain = (a.NA + kGatherAtoms - 1) / kGatherAtoms;
+    const int nmov = a.full ? 0 : a.n_mov_blocks;
+    k_gather<<<nmain + nmov, 2 * kGatherAtoms, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------
