@@ -196,6 +196,8 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     CUDA_CHECK(cudaStreamCreateWithFlags(&s_pme_, cudaStreamNonBlocking));
     CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
     CUDA_CHECK(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+    CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork2_, cudaEventDisableTiming));
+    CUDA_CHECK(cudaEventCreateWithFlags(&ev_join2_, cudaEventDisableTiming));
     CUDA_CHECK(cudaMallocHost(&h_pos_, sizeof(double) * 3 * (size_t)n_in_));
     CUDA_CHECK(cudaMallocHost(&h_forces_, sizeof(double) * 3 * (size_t)n_in_));
     CUDA_CHECK(cudaMallocHost(&h_fnb_, sizeof(double) * 3 * (size_t)n_in_));
@@ -232,6 +234,8 @@ Engine::~Engine() {
     cudaFreeHost(h_status_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
+    if (ev_fork2_) cudaEventDestroy(ev_fork2_);
+    if (ev_join2_) cudaEventDestroy(ev_join2_);
     if (s_main_) cudaStreamDestroy(s_main_);
     if (s_pme_) cudaStreamDestroy(s_pme_);
 }
@@ -525,6 +529,28 @@ void Engine::build_layout() {
             }
         }
         rd.row2_e = (int)row_desc_.size();
+    }
+    // Few rows (one or two replicas): each row's candidate blocks are split over
+    // up to 4 warps (parts), so that the list building is not one row's latency.
+    {
+        const int base_rows = (int)row_desc_.size();
+        int parts = base_rows > 0 ? sms_ * find_warps_per_sm() / base_rows : 1;
+        parts = std::max(1, std::min(4, parts));
+        if (parts > 1) {
+            std::vector<int4> split;
+            split.reserve((size_t)base_rows * parts);
+            for (const int4& d : row_desc_)
+                for (int p = 0; p < parts; p++) split.push_back(make_int4(d.x, d.y, d.z, p | (parts << 8)));
+            row_desc_.swap(split);
+            for (int r = 0; r < R_; r++) {
+                RepDev& rd = rep_host_[r];
+                rd.row1_b *= parts;
+                rd.row1_e *= parts;
+                rd.row2_b *= parts;
+                rd.row2_e *= parts;
+            }
+        }
+        row_parts_ = parts;
     }
     nrows_ = (int)row_desc_.size();
 
@@ -931,8 +957,18 @@ void Engine::record(cudaStream_t st, bool host_io) {
     if (!pme) launch_exceptions(a, st);
     if (pme && tune_pme_stream_) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
     launch_finalize(a, st);
-    launch_output(a, st);
-    launch_matrix(a, st);
+    if (pme && tune_pme_stream_) {
+        // the R x R matrix beside the force output
+        CUDA_CHECK(cudaEventRecord(ev_fork2_, st));
+        CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork2_, 0));
+        launch_matrix(a, s_pme_);
+        CUDA_CHECK(cudaEventRecord(ev_join2_, s_pme_));
+        launch_output(a, st);
+        CUDA_CHECK(cudaStreamWaitEvent(st, ev_join2_, 0));
+    } else {
+        launch_output(a, st);
+        launch_matrix(a, st);
+    }
     if (host_io) {
         CUDA_CHECK(cudaMemcpyAsync(h_results_, a.results, sizeof(double) * NUM_RES * (size_t)R_,
                                    cudaMemcpyDeviceToHost, st));

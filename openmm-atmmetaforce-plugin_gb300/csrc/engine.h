@@ -128,6 +128,7 @@ private:
     std::vector<int> in_off_;
     int n_in_ = 0;
     int NA_ = 0, NB_ = 0, nrows_ = 0;
+    int row_parts_ = 1;  // warps per tile-list row (1 unless rows are few)
     int row_cap_ = 96;
     int tile_cap_ = 0;
     int last_tiles_ = 0, last_max_row_ = 0;
@@ -185,7 +186,7 @@ private:
     std::vector<void*> d_allocs_;
 
     cudaStream_t s_main_ = nullptr, s_pme_ = nullptr;
-    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr, ev_fork2_ = nullptr, ev_join2_ = nullptr;
     cudaGraphExec_t graph_host_ = nullptr, graph_dev_ = nullptr;
     std::vector<KernelTime> times_;
 };

@@ -119,7 +119,7 @@ struct Args {
     float4* bb_c2;            // NB: state 2 (full mode)
     float4* bb_h2;
     // rows and tiles
-    const int4* row_desc;     // nrows: (I, kind, replica, 0)
+    const int4* row_desc;     // nrows: (I, kind, replica, part | parts << 8)
     int* row_count;           // nrows
     const int* ex_start;      // NB+1: exclusion tiles of row I (regular rows)
     const int2* ex_ent;       //   (J, mask id)
@@ -180,6 +180,7 @@ void launch_matrix(const Args& a, cudaStream_t s);
 void launch_adjoint(const Args& a, const double* g, double* dx, double* dd, double* dq, double* dsig, double* deps,
                     double* dpar, cudaStream_t s);
 int tiles_kernel_blocks_per_sm();
+int find_warps_per_sm();
 constexpr int kTileThreads = 256;
 
 }  // namespace atm

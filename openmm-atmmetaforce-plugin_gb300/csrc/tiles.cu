@@ -151,7 +151,7 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kin
 template <bool CUT>
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
                                          const int2* ee, int e0, int e1, int lane, int* out, int cap,
-                                         const float4* s_ipos, int& raw) {
+                                         const float4* s_ipos, int& raw, int first, int stride) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
@@ -163,8 +163,8 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
     bool over = false;
     raw = 0;
     const int jb = diff ? R.block_begin : I + 1;
-    for (int base = jb; base < R.block_end; base += 32) {
-        const int Jl = base + lane;
+    for (int base = jb + first; base < R.block_end; base += 32 * stride) {
+        const int Jl = base + lane * stride;
         bool ok = Jl < R.block_end;
         if (ok && diff) {
             const int cj = a.block_cls[Jl];
@@ -203,7 +203,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             float4 p[4];
 #pragma unroll
             for (int t = 0; t < 4; t++) {
-                J[t] = cand ? base + __ffs(cand) - 1 : -1;
+                J[t] = cand ? base + (__ffs(cand) - 1) * stride : -1;
                 if (cand) cand &= cand - 1;
             }
 #pragma unroll
@@ -250,6 +250,9 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
 __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* stage, float4* ipos) {
     const int4 d = a.row_desc[row];
     const int I = d.x, kind = d.y;
+    // part `part` of `nparts`: the candidate blocks J = first + part + k nparts;
+    // part 0 also holds the block tiles
+    const int part = d.w & 0xff, nparts = max(1, d.w >> 8);
     const RepDev& R = a.reps[d.z];
     const bool diff = kind >= ROW_DIFF1;
     const int* es = diff ? a.dx_start : a.ex_start;
@@ -269,15 +272,17 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     int raw = 0, natom = -1;
     if (!pbc) {
         load_ipos(a, R, I, kind, ci, lane, ipos);
-        natom = row_atoms<true>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw);
+        natom = row_atoms<true>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
+                                nparts);
     } else {
-        natom = row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw);
+        natom = row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
+                                 nparts);
         if (natom > kStageAtoms) natom = -1;
     }
     __syncwarp();
     const bool staged = natom >= 0;
     if (!staged) natom = raw;
-    const int nblock = e1 - e0;
+    const int nblock = part == 0 ? e1 - e0 : 0;
     const int natile = (natom + 31) / 32;
     int n = nblock + natile;
     if (lane == 0) atomicMax(&a.status->max_row, n);
@@ -299,7 +304,7 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
         for (int k = lane; k < natom; k += 32) out[k] = stage[k];
     } else {
         // second pass: the same atoms, in the same order, straight into the j slots
-        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom, ipos, raw);
+        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom, ipos, raw, part, nparts);
     }
     for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
     const int zword = row | (kind << 28);
@@ -332,6 +337,12 @@ __global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
         __syncwarp();
         k = __shfl_sync(FULL_MASK, mine, 0);
     }
+}
+
+int find_warps_per_sm() {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, kFindWarps * 32, 0);
+    return std::max(1, per_sm) * kFindWarps;
 }
 
 void launch_find(const Args& a, cudaStream_t s) {
