@@ -323,7 +323,7 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
 // state-2 / difference rows at the end of the row list scan every block of
 // their replica and are the longest, so they start early); the next row is
 // requested before the current one is built.
-__global__ void __launch_bounds__(kFindWarps * 32) k_find(Args a) {
+__global__ void __launch_bounds__(kFindWarps * 32, 6) k_find(Args a) {
     __shared__ int s_stage[kFindWarps][kStageAtoms];
     __shared__ float4 s_ipos[kFindWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -403,7 +403,10 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
                                            float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
                                            float crf, float3& fi, float3& fj, float& e32, double& e64) {
     const int src = (lane + 1) & 31;
-#pragma unroll 8
+    // the unmasked atom tiles carry most pairs; the other variants stay compact
+    // so that the hot loop keeps the instruction cache
+    constexpr int kUnroll = (!PBC && !DIFF && !MASKED) ? 8 : 2;
+#pragma unroll kUnroll
     for (int k = 0; k < 32; k++) {
         const float4 pj = sp[k];
         const float2 lj = sl[k];
@@ -443,7 +446,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
                                                float3& aj) {
     const int src = (lane + 1) & 31;
     const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
-#pragma unroll 4
+#pragma unroll 2
     for (int k = 0; k < 32; k++) {
         const float4 pj = sp[k];
         const float2 lj = sl[k];
