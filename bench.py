@@ -369,7 +369,7 @@ def main():
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
                 "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt, "tile_stats": batch.stats(),
-                "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 1024 * batch.stats()["tiles"]),
+                "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 256 * batch.stats()["tiles"]),
                 "issue": {"achieved": TILES_WARP_INSTR / t_tiles / 1e12,
                           "peak": props.multi_processor_count * 4 * sm_mhz * 1e6 / 1e12,
                           "unit": "T warp instructions/s",

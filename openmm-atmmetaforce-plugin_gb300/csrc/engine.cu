@@ -510,6 +510,49 @@ void Engine::build_layout() {
     dx_start_[NB_] = (int)dx_ent_.size();
     if (masks_.empty()) masks_.resize(32, 0xffffffffu);
 
+    // The pair-tile kernel works on half blocks (16 x 16 tiles).  Sub-tile (a, b)
+    // of exclusion tile (I, J) pairs atoms 16a .. 16a+15 of I with 16b .. 16b+15
+    // of J; its mask word l, bit k: pair (l, (l + k) & 15) is computed.  Of a
+    // diagonal tile: (0,0) and (1,1) (both orders, as the full tile) and (0,1);
+    // sub-tiles without a computed pair are dropped.
+    masks16_.clear();
+    exs_start_.assign(NB_ + 1, 0);
+    dxs_start_.assign(NB_ + 1, 0);
+    exs_ent_.clear();
+    dxs_ent_.clear();
+    auto add_subtiles = [&](int I, int J, int id, std::vector<int4>& out) {
+        for (int sa = 0; sa < 2; sa++)
+            for (int sb = 0; sb < 2; sb++) {
+                if (I == J && sa > sb) continue;
+                uint32_t m[kHalf];
+                bool any = false;
+                for (int l = 0; l < kHalf; l++) {
+                    const int ii = kHalf * sa + l;
+                    const uint32_t w = masks_[(size_t)id * 32 + ii];
+                    uint32_t v = 0;
+                    for (int k = 0; k < kHalf; k++) {
+                        const int jj = kHalf * sb + ((l + k) & (kHalf - 1));
+                        if ((w >> ((jj - ii) & 31)) & 1u) v |= 1u << k;
+                    }
+                    m[l] = v;
+                    any = any || v != 0;
+                }
+                if (!any) continue;
+                const int id16 = (int)(masks16_.size() / kHalf);
+                masks16_.insert(masks16_.end(), m, m + kHalf);
+                out.push_back(make_int4(2 * I + sa, 2 * J + sb, id16, 0));
+            }
+    };
+    for (int b = 0; b < NB_; b++) {
+        exs_start_[b] = (int)exs_ent_.size();
+        for (auto& e : blk_ex[b]) add_subtiles(b, e.first, e.second, exs_ent_);
+        dxs_start_[b] = (int)dxs_ent_.size();
+        for (auto& e : blk_dx[b]) add_subtiles(b, e.first, e.second, dxs_ent_);
+    }
+    exs_start_[NB_] = (int)exs_ent_.size();
+    dxs_start_[NB_] = (int)dxs_ent_.size();
+    if (masks16_.empty()) masks16_.resize(kHalf, 0xffffu);
+
     // rows: all state-1 rows, then state-2 rows (full) or the difference rows
     row_desc_.clear();
     for (int b = 0; b < NB_; b++) row_desc_.push_back(make_int4(b, ROW_STATE1, block_rep_[b], 0));
@@ -619,7 +662,7 @@ void Engine::build_layout() {
         rep_host_[r].e_disp = 0.0;
         if (s.dispersion) rep_host_[r].e_disp = dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]);
     }
-    if (tile_cap_ == 0) tile_cap_ = nrows_ * 28 + 4096;
+    if (tile_cap_ == 0) tile_cap_ = nrows_ * 56 + 8192;
     layout_ready_ = true;
 }
 
@@ -827,7 +870,11 @@ void Engine::alloc_device() {
     a.ex_ent = dupload(d_allocs_, ex_ent_);
     a.dx_start = dupload(d_allocs_, dx_start_);
     a.dx_ent = dupload(d_allocs_, dx_ent_);
-    a.masks = dupload(d_allocs_, masks_);
+    a.masks = dupload(d_allocs_, masks16_);
+    a.exs_start = dupload(d_allocs_, exs_start_);
+    a.exs_ent = dupload(d_allocs_, exs_ent_);
+    a.dxs_start = dupload(d_allocs_, dxs_start_);
+    a.dxs_ent = dupload(d_allocs_, dxs_ent_);
     a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
     a.tile_j = dalloc<int>(d_allocs_, 32 * (size_t)tile_cap_);
     a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
@@ -988,7 +1035,7 @@ bool Engine::check_status_and_grow() {
     if (!s.overflow) return false;
     if (s.overflow & 2) {
         int want = (int)(s.max_row * 1.25) + 8;
-        if (want > 1024) throw Error(6, "A tile row exceeds 1024 tiles: cutoff too large for the block layout");
+        if (want > 2040) throw Error(6, "A tile row exceeds 2040 tiles: cutoff too large for the block layout");
         row_cap_ = std::max(row_cap_, want);
     }
     if (s.overflow & 1) tile_cap_ = (int)(std::max(tile_cap_, s.tile_count) * 1.5) + 4096;

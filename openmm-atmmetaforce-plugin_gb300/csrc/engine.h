@@ -129,7 +129,7 @@ private:
     int n_in_ = 0;
     int NA_ = 0, NB_ = 0, nrows_ = 0;
     int row_parts_ = 1;  // warps per tile-list row (1 unless rows are few)
-    int row_cap_ = 96;
+    int row_cap_ = 192;
     int tile_cap_ = 0;
     int last_tiles_ = 0, last_max_row_ = 0;
     int method_ = 0;
@@ -151,7 +151,10 @@ private:
     std::vector<int4> row_desc_;
     std::vector<int> ex_start_, dx_start_;
     std::vector<int2> ex_ent_, dx_ent_;
-    std::vector<uint32_t> masks_;
+    std::vector<uint32_t> masks_;             // 32 x 32 exclusion masks (layout build)
+    std::vector<uint32_t> masks16_;           // 16 x 16 sub-tile masks (device)
+    std::vector<int> exs_start_, dxs_start_;  // per block: its exclusion sub-tiles
+    std::vector<int4> exs_ent_, dxs_ent_;     //   (I16, J16, mask16 id, 0)
     std::vector<int4> exc_ij_;
     std::vector<ExcParam> exc_p_;
     std::vector<int> exc_cta_first_;

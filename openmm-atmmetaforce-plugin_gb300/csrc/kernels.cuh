@@ -14,6 +14,7 @@
 namespace atm {
 
 constexpr int kTile = 32;
+constexpr int kHalf = 16;  // pair tiles are half blocks: 16 i atoms x 16 j slots
 constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr int kOrder = 5;  // PME B-spline order (OpenMM's)
 
@@ -125,7 +126,11 @@ struct Args {
     const int2* ex_ent;       //   (J, mask id)
     const int* dx_start;      // NB+1: cross-class exclusion tiles (difference rows)
     const int2* dx_ent;
-    const uint32_t* masks;    // 32 words per mask
+    const int* exs_start;     // NB+1: 16 x 16 sub-tiles of the exclusion tiles of row I
+    const int4* exs_ent;      //   (I16, J16, mask16 id, 0)
+    const int* dxs_start;     // NB+1: sub-tiles of the cross-class exclusion tiles
+    const int4* dxs_ent;
+    const uint32_t* masks;    // 16 words per mask (16 x 16 sub-tiles, low 16 bits)
     int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
     int tile_dynamic;         // 1: pair tiles handed out from a counter (large lists)
     int* tile_j;              // 32 j slots per tile (atom tiles)

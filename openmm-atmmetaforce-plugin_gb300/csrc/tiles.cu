@@ -97,10 +97,14 @@ __device__ __forceinline__ void load_ipos(const Args& a, const RepDev& R, int I,
 
 // Second cut of staged atoms list[from, natom): keeps the atoms j within the
 // cutoff of at least one atom of block I (the box test keeps every atom within
-// the cutoff of the box, corners included).  Positions are taken to the periodic
-// image nearest the box centre, as the pair-tile kernel does; the threshold is
-// widened by 1e-5 so that no pair the kernel counts can be dropped by rounding.
-// In place, order kept; returns from + the number kept.
+// the cutoff of the box, corners included), flagged by half block: bit 30 within
+// the cutoff of an atom 0..15 of I, bit 31 of an atom 16..31 (the pair tiles are
+// half blocks).  Positions are taken to the periodic image nearest the box
+// centre, as the pair-tile kernel does; the threshold is widened by 1e-5 so that
+// no pair the kernel counts can be dropped by rounding.  In place, order kept;
+// returns from + the number kept.
+constexpr unsigned kHalfA = 1u << 30, kHalfB = 1u << 31, kSlotBits = kHalfA - 1u;
+
 __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
                                          int from, int natom, const float4* s_ipos) {
     const float rc2 = a.rc2 * 1.00001f;
@@ -109,7 +113,7 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kin
         const int k = g + lane;
         const bool valid = k < natom;
         const int j = valid ? list[k] : 0;
-        bool hit = false;
+        bool hitA = false, hitB = false;
         float4 p = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);  // invalid lanes never hit
         if (valid) {
             p = row_pos(a, kind, j);
@@ -117,20 +121,31 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kin
             p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
             p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
         }
-        // eight i atoms at a time; stop once every lane has decided
-        for (int q0 = 0; q0 < 32; q0 += 8) {
+        // eight i atoms at a time; each half until every lane has decided it
+        for (int q0 = 0; q0 < kHalf; q0 += 8) {
 #pragma unroll
             for (int q = q0; q < q0 + 8; q++) {
                 const float4 o = s_ipos[q];
                 const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
-                hit |= dx * dx + dy * dy + dz * dz < rc2;
+                hitA |= dx * dx + dy * dy + dz * dz < rc2;
             }
-            if (__all_sync(FULL_MASK, hit || !valid)) break;
+            if (__all_sync(FULL_MASK, hitA || !valid)) break;
+        }
+        for (int q0 = kHalf; q0 < 32; q0 += 8) {
+#pragma unroll
+            for (int q = q0; q < q0 + 8; q++) {
+                const float4 o = s_ipos[q];
+                const float dx = p.x - o.x, dy = p.y - o.y, dz = p.z - o.z;
+                hitB |= dx * dx + dy * dy + dz * dz < rc2;
+            }
+            if (__all_sync(FULL_MASK, hitB || !valid)) break;
         }
         __syncwarp();
-        const bool keep = valid && hit;
+        const bool keep = valid && (hitA || hitB);
         const unsigned b = __ballot_sync(FULL_MASK, keep);
-        if (keep) list[kept + __popc(b & ((1u << lane) - 1u))] = j;
+        if (keep)
+            list[kept + __popc(b & ((1u << lane) - 1u))] =
+                (int)((unsigned)j | (hitA ? kHalfA : 0u) | (hitB ? kHalfB : 0u));
         kept += __popc(b);
         __syncwarp();
     }
@@ -281,10 +296,32 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     }
     __syncwarp();
     const bool staged = natom >= 0;
+    const bool flagged = staged && !pbc;  // cut atoms carry their half-block flags
     if (!staged) natom = raw;
-    const int nblock = part == 0 ? e1 - e0 : 0;
-    const int natile = (natom + 31) / 32;
-    int n = nblock + natile;
+    int nA = natom, nB = natom;  // uncut atoms go to both halves
+    if (flagged) {
+        nA = nB = 0;
+        for (int k = lane; k < natom; k += 32) {
+            const unsigned v = (unsigned)stage[k];
+            nA += (v & kHalfA) ? 1 : 0;
+            nB += (v & kHalfB) ? 1 : 0;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            nA += __shfl_xor_sync(FULL_MASK, nA, o);
+            nB += __shfl_xor_sync(FULL_MASK, nB, o);
+        }
+    }
+    // half-block tiles: the exclusion sub-tiles (part 0), then the atom tiles of
+    // each half; an even count, so that the two halves of a warp share a row
+    const int* ss = diff ? a.dxs_start : a.exs_start;
+    const int4* se = diff ? a.dxs_ent : a.exs_ent;
+    const int s0 = ss[I];
+    const int nblock = part == 0 ? ss[I + 1] - s0 : 0;
+    const int nta = (nA + kHalf - 1) / kHalf, ntb = (nB + kHalf - 1) / kHalf;
+    int n = nblock + nta + ntb;
+    const bool filler = n & 1;
+    n += filler ? 1 : 0;
     if (lane == 0) atomicMax(&a.status->max_row, n);
     if (n > a.row_cap) {
         if (lane == 0) atomicOr(&a.status->overflow, 2);
@@ -299,24 +336,47 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
         if (lane == 0) atomicOr(&a.status->overflow, 1);
         return;
     }
-    int* out = a.tile_j + (size_t)(tbase + nblock) * 32;
-    if (staged) {
-        for (int k = lane; k < natom; k += 32) out[k] = stage[k];
+    int* outA = a.tile_j + (size_t)(tbase + nblock) * kHalf;
+    int* outB = outA + (size_t)nta * kHalf;
+    if (flagged) {
+        int ka = 0, kb = 0;
+        for (int g = 0; g < natom; g += 32) {
+            const int k = g + lane;
+            const unsigned v = k < natom ? (unsigned)stage[k] : 0u;
+            const bool fa = v & kHalfA, fb = v & kHalfB;
+            const unsigned ba = __ballot_sync(FULL_MASK, fa), bb = __ballot_sync(FULL_MASK, fb);
+            const unsigned lt = (1u << lane) - 1u;
+            if (fa) outA[ka + __popc(ba & lt)] = (int)(v & kSlotBits);
+            if (fb) outB[kb + __popc(bb & lt)] = (int)(v & kSlotBits);
+            ka += __popc(ba);
+            kb += __popc(bb);
+        }
+    } else if (staged) {
+        for (int k = lane; k < natom; k += 32) {
+            outA[k] = stage[k];
+            outB[k] = stage[k];
+        }
     } else {
-        // second pass: the same atoms, in the same order, straight into the j slots
-        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, out, natom, ipos, raw, part, nparts);
+        // second pass: the same atoms, in the same order, straight into the j slots of both halves
+        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outA, natom, ipos, raw, part, nparts);
+        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outB, natom, ipos, raw, part, nparts);
     }
-    for (int k = natom + lane; k < 32 * natile; k += 32) out[k] = -1;
+    for (int k = nA + lane; k < kHalf * nta; k += 32) outA[k] = -1;
+    for (int k = nB + lane; k < kHalf * ntb; k += 32) outB[k] = -1;
     const int zword = row | (kind << 28);
     for (int k = lane; k < nblock; k += 32) {
-        const int2 e = ee[e0 + k];
-        a.tiles[tbase + k] = make_int4(I, e.x, zword, (int)((unsigned)(e.y + 1) | ((unsigned)k << 20) | (1u << 31)));
+        const int4 e = se[s0 + k];
+        a.tiles[tbase + k] = make_int4(e.x, e.y, zword, (int)((unsigned)(e.z + 1) | ((unsigned)k << 20) | (1u << 31)));
     }
-    for (int k = lane; k < natile; k += 32) {
-        const int cnt = min(32, natom - 32 * k);
-        a.tiles[tbase + nblock + k] =
-            make_int4(I, 0, zword | (1 << 30), (int)((unsigned)cnt | ((unsigned)(nblock + k) << 20) | (pbc << 31)));
+    for (int k = lane; k < nta + ntb; k += 32) {
+        const bool hb = k >= nta;
+        const int kk = hb ? k - nta : k;
+        const int cnt = min(kHalf, (hb ? nB : nA) - kHalf * kk);
+        a.tiles[tbase + nblock + k] = make_int4(2 * I + (hb ? 1 : 0), 0, zword | (1 << 30),
+                                                (int)((unsigned)cnt | ((unsigned)(nblock + k) << 20) | (pbc << 31)));
     }
+    if (filler && lane == 0)  // an empty atom tile (no j), energy slot n - 1
+        a.tiles[tbase + n - 1] = make_int4(2 * I, 0, zword | (1 << 30), (int)((unsigned)(n - 1) << 20));
 }
 
 // Persistent: every warp takes rows from a counter, last rows first (the
@@ -392,22 +452,23 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
     }
 }
 
-// The 32 steps of one tile: lane l meets j-slot (l+k)&31 at step k; j data are
-// read from shared memory (stored twice over, so that slot (l+k)&31 is entry l+k
-// of the lane's own base: a constant offset per unrolled step), j forces travel
-// with their slot by warp shuffles.  MASKED: a per-lane bit mask of the pairs to
+// The 16 steps of one half-block tile, on each half of the warp: lane l of a
+// half meets j-slot (l+k)&15 at step k; j data are read from shared memory
+// (stored twice over, so that slot (l+k)&15 is entry l+k of the lane's own base:
+// a constant offset per unrolled step), j forces travel with their slot by
+// shuffles within the half.  MASKED: a per-lane bit mask of the pairs to
 // count (exclusions, padding); unmasked tiles park their padding j slots far away.
 template <int METHOD, bool PBC, bool DIFF, bool MASKED>
 __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
                                            float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
                                            float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
                                            float crf, float3& fi, float3& fj, float& e32, double& e64) {
-    const int src = (lane + 1) & 31;
+    const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     // the unmasked atom tiles carry most pairs; the other variants stay compact
     // so that the hot loop keeps the instruction cache
     constexpr int kUnroll = (!PBC && !DIFF && !MASKED) ? 8 : 2;
 #pragma unroll kUnroll
-    for (int k = 0; k < 32; k++) {
+    for (int k = 0; k < kHalf; k++) {
         const float4 pj = sp[k];
         const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
@@ -444,10 +505,10 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
                                                float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
                                                float crf, float3& fi, float3& fj, double& e64, float3& ai,
                                                float3& aj) {
-    const int src = (lane + 1) & 31;
+    const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
 #pragma unroll 2
-    for (int k = 0; k < 32; k++) {
+    for (int k = 0; k < kHalf; k++) {
         const float4 pj = sp[k];
         const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
@@ -501,22 +562,26 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     __shared__ float4 s_p[kTileThreads / 32][64];
     __shared__ float2 s_l[kTileThreads / 32][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int hf = lane >> 4, l = lane & (kHalf - 1);  // half of the warp, lane within it
     int ntiles = a.status->tile_count;
     if (ntiles > a.tile_cap) ntiles = a.tile_cap;
+    const int npairs = ntiles >> 1;  // every row holds an even number of tiles
     const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
-    // Large lists: tiles handed out kTileGrab at a time from a counter (the next
-    // grab requested before the current tiles are processed), so that warps finish
-    // together.  Small lists (a few tiles per warp): warp w takes tiles w, w + nw, ...
+    // A warp takes two consecutive tiles (one per half; the same row).  Large
+    // lists: pairs handed out kTileGrab at a time from a counter (the next grab
+    // requested before the current pairs are processed), so that warps finish
+    // together.  Small lists (a few pairs per warp): warp w takes pairs w, w + nw, ...
     // (DYN, chosen by the host from the size of the row list)
     int mine = 0;
     if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
     int cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    while (cur < ntiles) {
+    while (cur < npairs) {
     if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
-    const int cur_end = DYN ? min(cur + kTileGrab, ntiles) : cur + 1;
-    for (int t = cur; t < cur_end; t++) {
+    const int cur_end = DYN ? min(cur + kTileGrab, npairs) : cur + 1;
+    for (int pq = cur; pq < cur_end; pq++) {
+        const int t = 2 * pq + hf;
         const int4 T = a.tiles[t];
-        const int I = T.x;
+        const int I16 = T.x, I = I16 >> 1;
         const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
         const int row = z & 0x0fffffffu, kind = (z >> 28) & 3u;
         const bool atom_tile = (z >> 30) & 1u;
@@ -527,21 +592,20 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         const float iLx = R.ibox[0], iLy = R.ibox[1], iLz = R.ibox[2];
         const bool diff = kind >= ROW_DIFF1, g2 = kind == ROW_DIFF2;
         const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
-        const int i = I * kTile + lane;
+        const int i = I16 * kHalf + l;
         float4 pi = P[i];
         const float2 li = a.lj[i];
         int j;
         unsigned mask;
         bool jvalid = true;
         if (atom_tile) {
-            j = a.tile_j[(size_t)t * 32 + lane];
-            const unsigned vb = aux >= 32 ? FULL_MASK : ((1u << aux) - 1u);
-            mask = __funnelshift_r(vb, vb, lane);  // bit k: j-slot (lane+k)&31 is a real atom
-            jvalid = lane < aux;
-            if (!jvalid) j = i;
+            jvalid = l < aux;
+            j = jvalid ? a.tile_j[(size_t)t * kHalf + l] : i;
+            const unsigned vb = aux >= kHalf ? 0xffffu : ((1u << aux) - 1u);
+            mask = ((vb >> l) | (vb << (kHalf - l))) & 0xffffu;  // bit k: j-slot (l+k)&15 is a real atom
         } else {
-            j = T.y * kTile + lane;
-            mask = a.masks[(size_t)(aux - 1) * 32 + lane];
+            j = T.y * kHalf + l;
+            mask = a.masks[(size_t)(aux - 1) * kHalf + l];
         }
         float4 pj = P[j];
         const float2 lj = a.lj[j];
@@ -566,30 +630,34 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
             pi.z = c.z + min_img(pi.z - c.z, Lz, iLz);
         }
         // atom tiles without per-pair minimum images need no mask: padding j slots
-        // are parked far beyond the cutoff
-        const bool masked = !atom_tile || pbc;
-        if (!masked && !jvalid) pj.x = pj.y = pj.z = 1.0e15f;
-        s_p[w][lane] = pj;
-        s_p[w][lane + 32] = pj;
-        s_l[w][lane] = lj;
-        s_l[w][lane + 32] = lj;
+        // are parked far beyond the cutoff.  The variant is the warp's: masked or
+        // per-pair images when either half needs it (the same pairs and arithmetic
+        // for the other half).  Both halves are of one row, so of one kind.
+        const bool masked_h = !atom_tile || pbc;
+        if (!masked_h && !jvalid) pj.x = pj.y = pj.z = 1.0e15f;
+        const bool masked = __any_sync(FULL_MASK, masked_h);
+        const bool pbc_w = __any_sync(FULL_MASK, pbc);
+        s_p[w][32 * hf + l] = pj;
+        s_p[w][32 * hf + l + kHalf] = pj;
+        s_l[w][32 * hf + l] = lj;
+        s_l[w][32 * hf + l + kHalf] = lj;
         __syncwarp();
-        const float4* spl = &s_p[w][lane];
-        const float2* sll = &s_l[w][lane];
+        const float4* spl = &s_p[w][32 * hf + l];
+        const float2* sll = &s_l[w][32 * hf + l];
         float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
         float3 ai = make_float3(0.f, 0.f, 0.f), aj = make_float3(0.f, 0.f, 0.f);
         float e32 = 0.f;
         double e64 = 0.0;
         const bool adj = diff && a.adjoint;
         if (adj) {
-            if (pbc)
+            if (pbc_w)
                 tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
                                              crf, fi, fj, e64, ai, aj);
             else
                 tile_steps_adj<METHOD, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
                                               crf, fi, fj, e64, ai, aj);
         } else if (diff) {
-            if (pbc)
+            if (pbc_w)
                 tile_steps<METHOD, true, true, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
                                                      alpha, krf, crf, fi, fj, e32, e64);
             else if (masked)
@@ -599,7 +667,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
                 tile_steps<METHOD, false, true, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
                                                        alpha, krf, crf, fi, fj, e32, e64);
         } else {
-            if (pbc)
+            if (pbc_w)
                 tile_steps<METHOD, true, false, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
                                                       alpha, krf, crf, fi, fj, e32, e64);
             else if (masked)
@@ -610,22 +678,23 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
                                                         alpha, krf, crf, fi, fj, e32, e64);
         }
         __syncwarp();
-        const bool diag = !atom_tile && T.y == I;
-        // tile energy: FP64 on the difference tiles (their sum is u), FP32 over the
-        // lanes otherwise (FP64 arithmetic is scarce on this part); fixed order either way
+        const bool diag = !atom_tile && T.y == I16;
+        // tile energy over the half: FP64 on the difference tiles (their sum is u),
+        // FP32 otherwise (FP64 arithmetic is scarce on this part); fixed order either way
         double esum;
         if (diff) {
             esum = e64;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+            for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
         } else {
             float es = diag ? 0.5f * e32 : e32;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
+            for (int o = kHalf / 2; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
             esum = (double)es;
         }
         const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
-        if (lane == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
+        if (l == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
+        if (!atom_tile || aux > 0) {  // (an empty tile, the filler of an odd row, adds nothing)
         unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
         fix_add_t(Fp + i, sign * fi.x);
         fix_add_t(Fp + a.NA + i, sign * fi.y);
@@ -645,6 +714,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
                 fix_add_t(D + a.NA + j, sign * aj.y);
                 fix_add_t(D + 2 * (size_t)a.NA + j, sign * aj.z);
             }
+        }
         }
     }
     cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : cur + ((gridDim.x * blockDim.x) >> 5);
