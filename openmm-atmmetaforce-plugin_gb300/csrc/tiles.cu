@@ -2,22 +2,26 @@
 // Ewald) of the ATM evaluation path, sm_103a.
 //
 // A "row" is one 32-atom block I at one geometry (state 1, state 2, or one of the
-// two geometries of the ligand-difference tiles).  k_find builds, per row:
-//   - block tiles: (I, J) for the diagonal tile and every block pair holding an
-//     exclusion, with a 32 x 32 exclusion mask;
+// two geometries of the ligand-difference tiles); its candidate blocks may be split
+// over several rows (parts) when rows are few.  Tiles are half blocks: 16 i atoms
+// (I16 = 2 I or 2 I + 1) by 16 j slots.  k_find builds, per row:
+//   - exclusion sub-tiles: the 16 x 16 sub-tiles with a computed pair of the
+//     diagonal tile and of every block pair holding an exclusion, with masks;
 //   - atom tiles: the atoms j of every other candidate block J (bounding boxes
 //     closer than the cutoff) that lie within the cutoff of block I's bounding
-//     box and then within the cutoff of at least one atom of block I, packed 32
-//     per tile.
-// The per-atom tests remove most of the pair slots a 32 x 32 block tile would
-// spend beyond the cutoff.
+//     box and then within the cutoff of at least one atom of a half block, packed
+//     16 per tile of that half;
+//   - an even number of tiles (an empty atom tile fills an odd count), so that the
+//     two halves of a warp in the pair-tile kernel always hold tiles of one row.
+// The per-atom tests remove most of the pair slots a block tile would spend beyond
+// the cutoff.
 //
 // Tile entry (int4):
-//   x = I
-//   y = J (block tiles)
+//   x = I16
+//   y = J16 (exclusion sub-tiles)
 //   z = row | kind << 28 | atom_tile << 30
 //   w = aux | slot << 20 | pbc << 31
-//       aux  = mask id + 1 (block tiles) or number of valid j (atom tiles)
+//       aux  = mask id + 1 (sub-tiles) or number of valid j (atom tiles, 0: filler)
 //       slot = position of the tile within its row (energy slot)
 //       pbc  = 1 when every pair needs its own minimum image (small boxes)
 #include <algorithm>
