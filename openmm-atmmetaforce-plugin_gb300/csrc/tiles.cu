@@ -26,6 +26,8 @@
 //       pbc  = 1 when every pair needs its own minimum image (small boxes)
 #include <algorithm>
 
+#include <cuda_fp16.h>
+
 #include "kernels.cuh"
 
 namespace atm {
@@ -88,16 +90,41 @@ __device__ __forceinline__ float4 row_pos(const Args& a, int kind, int s) {
 
 // Positions of the atoms of block I at the geometry of a row, taken to the
 // periodic image nearest the box centre (as the pair-tile kernel does), into the
-// warp's shared memory for the exact cut.
+// warp's shared memory for the exact cut: FP32 (absolute), or with hcut the
+// offsets from the box centre as half2 pairs (atoms 2m, 2m+1: x, y, z; 16 bytes
+// per pair, in the first half of the same buffer).
 __device__ __forceinline__ void load_ipos(const Args& a, const RepDev& R, int I, int kind, float4 ci, int lane,
-                                          float4* s_ipos) {
-    float4 pi = row_pos(a, kind, I * kTile + lane);
-    pi.x = ci.x + min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
-    pi.y = ci.y + min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
-    pi.z = ci.z + min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
-    s_ipos[lane] = pi;
+                                          float4* s_ipos, bool hcut) {
+    const float4 pi = row_pos(a, kind, I * kTile + lane);
+    const float rx = min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
+    const float ry = min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
+    const float rz = min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
+    if (hcut) {
+        const float nx = __shfl_down_sync(FULL_MASK, rx, 1), ny = __shfl_down_sync(FULL_MASK, ry, 1),
+                    nz = __shfl_down_sync(FULL_MASK, rz, 1);
+        if ((lane & 1) == 0) {
+            const __half2 hx = __floats2half2_rn(rx, nx), hy = __floats2half2_rn(ry, ny), hz = __floats2half2_rn(rz, nz);
+            uint4 q;
+            q.x = *reinterpret_cast<const unsigned*>(&hx);
+            q.y = *reinterpret_cast<const unsigned*>(&hy);
+            q.z = *reinterpret_cast<const unsigned*>(&hz);
+            q.w = 0u;
+            reinterpret_cast<uint4*>(s_ipos)[lane >> 1] = q;
+        }
+    } else {
+        s_ipos[lane] = make_float4(ci.x + rx, ci.y + ry, ci.z + rz, pi.w);
+    }
     __syncwarp();
 }
+
+// Rows whose block box is at most kHalfCutMaxH (nm) in every dimension, with a
+// cutoff of at most kHalfCutMaxRc, take the half-precision exact cut.  Offsets
+// from the box centre are then below 2.25 nm (rounded by <= 2^-10 nm) and a pair
+// near the cutoff has |dx| <= 1.5 nm per component, so each component of the
+// half difference is off by <= 0.0017 nm and r^2 by <= 0.0117 nm^2 with the
+// roundings of the products: r by <= 0.004 nm.  The cut distance is widened by
+// kHalfCutMargin, so no pair within the cutoff of the FP32 kernel is lost.
+constexpr float kHalfCutMaxH = 0.75f, kHalfCutMaxRc = 1.5f, kHalfCutMargin = 0.005f;
 
 // Second cut of staged atoms list[from, natom): keeps the atoms j within the
 // cutoff of at least one atom of block I (the box test keeps every atom within
@@ -109,8 +136,65 @@ __device__ __forceinline__ void load_ipos(const Args& a, const RepDev& R, int I,
 // returns from + the number kept.
 constexpr unsigned kHalfA = 1u << 30, kHalfB = 1u << 31, kSlotBits = kHalfA - 1u;
 
+__device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, int kind, float4 ci, int lane,
+                                              int* list, int from, int natom, const float4* s_ipos) {
+    const float rcm = sqrtf(a.rc2) + kHalfCutMargin;
+    const __half2 thr = __float2half2_rn(rcm * rcm);
+    const uint4* ih = reinterpret_cast<const uint4*>(s_ipos);
+    int kept = from;
+    for (int g = from; g < natom; g += 32) {
+        const int k = g + lane;
+        const bool valid = k < natom;
+        const int j = valid ? list[k] : 0;
+        float rx = 64.f, ry = 64.f, rz = 64.f;  // invalid lanes never hit
+        if (valid) {
+            const float4 p = row_pos(a, kind, j);
+            rx = min_img(p.x - ci.x, R.box[0], R.ibox[0]);
+            ry = min_img(p.y - ci.y, R.box[1], R.ibox[1]);
+            rz = min_img(p.z - ci.z, R.box[2], R.ibox[2]);
+        }
+        const __half2 hx = __float2half2_rn(rx), hy = __float2half2_rn(ry), hz = __float2half2_rn(rz);
+        bool hitA = false, hitB = false;
+        // two i atoms per instruction, eight per step; each half until every lane has decided it
+        for (int m0 = 0; m0 < kHalf / 2; m0 += 4) {
+#pragma unroll
+            for (int m = m0; m < m0 + 4; m++) {
+                const uint4 q = ih[m];
+                const __half2 dx = __hsub2(hx, *reinterpret_cast<const __half2*>(&q.x));
+                const __half2 dy = __hsub2(hy, *reinterpret_cast<const __half2*>(&q.y));
+                const __half2 dz = __hsub2(hz, *reinterpret_cast<const __half2*>(&q.z));
+                const __half2 r2 = __hfma2(dx, dx, __hfma2(dy, dy, __hmul2(dz, dz)));
+                hitA |= !__hbge2(r2, thr);  // either atom of the pair within the widened cutoff
+            }
+            if (__all_sync(FULL_MASK, hitA || !valid)) break;
+        }
+        for (int m0 = kHalf / 2; m0 < kHalf; m0 += 4) {
+#pragma unroll
+            for (int m = m0; m < m0 + 4; m++) {
+                const uint4 q = ih[m];
+                const __half2 dx = __hsub2(hx, *reinterpret_cast<const __half2*>(&q.x));
+                const __half2 dy = __hsub2(hy, *reinterpret_cast<const __half2*>(&q.y));
+                const __half2 dz = __hsub2(hz, *reinterpret_cast<const __half2*>(&q.z));
+                const __half2 r2 = __hfma2(dx, dx, __hfma2(dy, dy, __hmul2(dz, dz)));
+                hitB |= !__hbge2(r2, thr);
+            }
+            if (__all_sync(FULL_MASK, hitB || !valid)) break;
+        }
+        __syncwarp();
+        const bool keep = valid && (hitA || hitB);
+        const unsigned b = __ballot_sync(FULL_MASK, keep);
+        if (keep)
+            list[kept + __popc(b & ((1u << lane) - 1u))] =
+                (int)((unsigned)j | (hitA ? kHalfA : 0u) | (hitB ? kHalfB : 0u));
+        kept += __popc(b);
+        __syncwarp();
+    }
+    return kept;
+}
+
 __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
-                                         int from, int natom, const float4* s_ipos) {
+                                         int from, int natom, const float4* s_ipos, bool hcut) {
+    if (hcut) return exact_cut_half(a, R, kind, ci, lane, list, from, natom, s_ipos);
     const float rc2 = a.rc2 * 1.00001f;
     int kept = from;
     for (int g = from; g < natom; g += 32) {
@@ -170,7 +254,8 @@ __device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kin
 template <bool CUT>
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
                                          const int2* ee, int e0, int e1, int lane, int* out, int cap,
-                                         const float4* s_ipos, int& raw, int first, int stride) {
+                                         const float4* s_ipos, int& raw, int first, int stride,
+                                         bool hcut = false) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
@@ -251,7 +336,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             }
             if (CUT && !over && natom > cap - 4 * kTile) {
                 __syncwarp();
-                natom = exact_cut(a, R, kind, ci, lane, out, cut_from, min(natom, cap), s_ipos);
+                natom = exact_cut(a, R, kind, ci, lane, out, cut_from, min(natom, cap), s_ipos, hcut);
                 cut_from = natom;
                 over = natom > cap - 4 * kTile;
             }
@@ -260,7 +345,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
     if (CUT) {
         if (over) return -1;
         __syncwarp();
-        natom = exact_cut(a, R, kind, ci, lane, out, cut_from, natom, s_ipos);
+        natom = exact_cut(a, R, kind, ci, lane, out, cut_from, natom, s_ipos, hcut);
     }
     return natom;
 }
@@ -290,9 +375,10 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     // that need per-pair images (no exact cut), are written by a second pass
     int raw = 0, natom = -1;
     if (!pbc) {
-        load_ipos(a, R, I, kind, ci, lane, ipos);
+        const bool hcut = rc <= kHalfCutMaxRc && fmaxf(hi.x, fmaxf(hi.y, hi.z)) <= kHalfCutMaxH;
+        load_ipos(a, R, I, kind, ci, lane, ipos, hcut);
         natom = row_atoms<true>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
-                                nparts);
+                                nparts, hcut);
     } else {
         natom = row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
                                  nparts);
