@@ -192,7 +192,7 @@ __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, in
     return kept;
 }
 
-__device__ __forceinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
+__device__ __noinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
                                          int from, int natom, const float4* s_ipos, bool hcut) {
     if (hcut) return exact_cut_half(a, R, kind, ci, lane, list, from, natom, s_ipos);
     const float rc2 = a.rc2 * 1.00001f;
