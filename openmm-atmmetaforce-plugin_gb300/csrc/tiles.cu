@@ -668,9 +668,18 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     while (cur < npairs) {
     if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
     const int cur_end = DYN ? min(cur + kTileGrab, npairs) : cur + 1;
+    // the tile entry and the j slot of the next pass are loaded before this
+    // pass's pair loop, so that their latency is hidden behind it
+    int4 Tn = a.tiles[2 * cur + hf];
+    int jn = a.tile_j[(size_t)(2 * cur + hf) * kHalf + l];
     for (int pq = cur; pq < cur_end; pq++) {
         const int t = 2 * pq + hf;
-        const int4 T = a.tiles[t];
+        const int4 T = Tn;
+        const int jraw = jn;
+        if (pq + 1 < cur_end) {
+            Tn = a.tiles[t + 2];
+            jn = a.tile_j[(size_t)(t + 2) * kHalf + l];
+        }
         const int I16 = T.x, I = I16 >> 1;
         const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
         const int row = z & 0x0fffffffu, kind = (z >> 28) & 3u;
@@ -690,7 +699,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         bool jvalid = true;
         if (atom_tile) {
             jvalid = l < aux;
-            j = jvalid ? a.tile_j[(size_t)t * kHalf + l] : i;
+            j = jvalid ? jraw : i;
             const unsigned vb = aux >= kHalf ? 0xffffu : ((1u << aux) - 1u);
             mask = ((vb >> l) | (vb << (kHalf - l))) & 0xffffu;  // bit k: j-slot (l+k)&15 is a real atom
         } else {
