@@ -494,6 +494,9 @@ MDDriver::MDDriver(const std::vector<const System*>& systems, int device, bool f
     for (int r = 0; r < R_; r++) in_off_.push_back(eng_->in_offset(r));
     MD_CHECK(cudaSetDevice(dev_));
     MD_CHECK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+    MD_CHECK(cudaStreamCreateWithFlags(&s_terms_, cudaStreamNonBlocking));
+    MD_CHECK(cudaEventCreateWithFlags(&ev_x_, cudaEventDisableTiming));
+    MD_CHECK(cudaEventCreateWithFlags(&ev_terms_, cudaEventDisableTiming));
     upload_terms(systems);
     update_beta();
 }
@@ -504,6 +507,9 @@ MDDriver::~MDDriver() {
     if (rec_mat_) cudaFree(rec_mat_);
     for (void* p : allocs_) cudaFree(p);
     if (s_) cudaStreamDestroy(s_);
+    if (s_terms_) cudaStreamDestroy(s_terms_);
+    if (ev_x_) cudaEventDestroy(ev_x_);
+    if (ev_terms_) cudaEventDestroy(ev_terms_);
 }
 
 void MDDriver::upload_terms(const std::vector<const System*>& systems) {
@@ -830,15 +836,21 @@ int MDDriver::get_records(long long* steps, double* results, double* matrices, i
 void MDDriver::compute_forces() {
     if (!have_positions_) throw Error(3, "Positions have not been set");
     MD_CHECK(cudaSetDevice(dev_));
-    MD_CHECK(cudaMemsetAsync(fb_, 0, sizeof(unsigned long long) * 3 * (size_t)n_, s_));
+    // the group-0 terms on their own stream, beside the ATM evaluation (after the
+    // positions are final; joined before anything on s_ reads their forces)
+    MD_CHECK(cudaEventRecord(ev_x_, s_));
+    MD_CHECK(cudaStreamWaitEvent(s_terms_, ev_x_, 0));
+    MD_CHECK(cudaMemsetAsync(fb_, 0, sizeof(unsigned long long) * 3 * (size_t)n_, s_terms_));
     {
         MdDev a = dev_args();
         int nt = n_bonds_ + n_angles_ + n_posres_;
-        if (nt > 0) k_md_terms<<<(nt + 127) / 128, 128, 0, s_>>>(a);
-        if (n_cent_ > 0) k_md_centroid<<<n_cent_, 128, 0, s_>>>(a);
+        if (nt > 0) k_md_terms<<<(nt + 127) / 128, 128, 0, s_terms_>>>(a);
+        if (n_cent_ > 0) k_md_centroid<<<n_cent_, 128, 0, s_terms_>>>(a);
         MD_CHECK(cudaGetLastError());
     }
+    MD_CHECK(cudaEventRecord(ev_terms_, s_terms_));
     eng_->run_device(x_, s_);  // ends with a synchronisation of s_
+    MD_CHECK(cudaStreamWaitEvent(s_, ev_terms_, 0));
     forces_valid_ = true;
     // re-sort when the pair-tile count shows the atom order has decayed
     int tiles = 0;
@@ -885,6 +897,7 @@ void MDDriver::get_state(double* pos, double* vel, double* forces, double* poten
                          double* results) {
     MD_CHECK(cudaSetDevice(dev_));
     if ((forces || potential || kinetic || results) && !forces_valid_) compute_forces();
+    MD_CHECK(cudaStreamSynchronize(s_terms_));  // the group-0 forces and energies below
     if (pos) MD_CHECK(cudaMemcpy(pos, x_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToHost));
     if (vel) MD_CHECK(cudaMemcpy(vel, v_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToHost));
     if (forces) {

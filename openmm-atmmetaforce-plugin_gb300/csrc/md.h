@@ -124,6 +124,8 @@ private:
     std::vector<int> dof_;  // per replica: 3 x moving atoms - constraints
 
     cudaStream_t s_ = nullptr;
+    cudaStream_t s_terms_ = nullptr;  // group-0 terms, beside the ATM evaluation
+    cudaEvent_t ev_x_ = nullptr, ev_terms_ = nullptr;
     std::vector<void*> allocs_;
     double *x_ = nullptr, *v_ = nullptr, *xn_ = nullptr, *inv_m_ = nullptr;
     int* rep_of_ = nullptr;
