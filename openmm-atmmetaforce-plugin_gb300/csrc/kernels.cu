@@ -408,9 +408,9 @@ __device__ __forceinline__ void spread_candidates(const Args& a, const RepDev& R
         const int s = Jc * kTile + lane;
         const int nreal = __float_as_int(a.bb_h[Jc].w);
         float4 p = code == 2 ? a.posq2[s] : a.posq[s];
-        const float4 dd = a.displ[s];
         if (code == 1) p.w = -p.w;
         if (code == 3) {
+            const float4 dd = a.displ[s];
             p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
             p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
             p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
