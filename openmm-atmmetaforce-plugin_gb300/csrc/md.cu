@@ -26,6 +26,7 @@ struct MdDev {
     double* v;
     double* xn;
     const double* inv_m;
+    const double* sqrt_inv_m;  // per atom, for the thermostat noise
     const int* rep_of;
     const double* f_atm;
     unsigned long long* fb;
@@ -202,13 +203,15 @@ __global__ void k_md_integrate(MdDev a) {
     const int r = a.rep_of[i];
     normals3((uint32_t)(i - a.rep_off[r]), a.step_lo, a.step_hi, ((uint32_t)r << 1) | RNG_THERMOSTAT, a.seed_lo,
              a.seed_hi, z);
-    double sim = sqrt(im);
+    // FP64 is scarce on this part: per-atom factors once, then four fused
+    // multiply-adds per component
+    const double fim = a.fscale * im, nsim = a.noisescale * a.sqrt_inv_m[i];
     for (int k = 0; k < 3; k++) {
         size_t o = 3 * (size_t)i + k;
-        double f = a.f_atm[o] + fix_to_d(a.fb[o]);
-        double v = a.vscale * a.v[o] + a.fscale * f * im + a.noisescale * sim * z[k];
+        const double f = fma((double)(long long)a.fb[o], 1.0 / kFixScale, a.f_atm[o]);
+        const double v = fma(nsim, z[k], fma(fim, f, a.vscale * a.v[o]));
         a.v[o] = v;
-        a.xn[o] = a.x[o] + a.dt * v;
+        a.xn[o] = fma(a.dt, v, a.x[o]);
     }
 }
 
@@ -679,6 +682,11 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
     xn_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
     MD_CHECK(cudaMemset(v_, 0, sizeof(double) * 3 * (size_t)n_));
     inv_m_ = md_upload(allocs_, inv_m);
+    {
+        std::vector<double> sq(n_);
+        for (int i = 0; i < n_; i++) sq[i] = std::sqrt(inv_m[i]);
+        sqrt_inv_m_ = md_upload(allocs_, sq);
+    }
     rep_of_ = md_upload(allocs_, rep_of);
     fb_ = md_alloc<unsigned long long>(allocs_, 3 * (size_t)n_);
     MD_CHECK(cudaMemset(fb_, 0, sizeof(unsigned long long) * 3 * (size_t)n_));
@@ -707,6 +715,7 @@ MdDev MDDriver::dev_args() const {
     a.v = v_;
     a.xn = xn_;
     a.inv_m = inv_m_;
+    a.sqrt_inv_m = sqrt_inv_m_;
     a.rep_of = rep_of_;
     a.f_atm = eng_->forces_device();
     a.fb = fb_;

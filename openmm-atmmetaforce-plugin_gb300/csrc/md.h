@@ -127,7 +127,7 @@ private:
     cudaStream_t s_terms_ = nullptr;  // group-0 terms, beside the ATM evaluation
     cudaEvent_t ev_x_ = nullptr, ev_terms_ = nullptr;
     std::vector<void*> allocs_;
-    double *x_ = nullptr, *v_ = nullptr, *xn_ = nullptr, *inv_m_ = nullptr;
+    double *x_ = nullptr, *v_ = nullptr, *xn_ = nullptr, *inv_m_ = nullptr, *sqrt_inv_m_ = nullptr;
     int* rep_of_ = nullptr;
     unsigned long long* fb_ = nullptr;  // group-0 forces, 3n fixed point
     double* e_terms_ = nullptr;         // one energy per term
