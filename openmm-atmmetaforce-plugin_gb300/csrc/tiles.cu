@@ -508,10 +508,31 @@ void launch_find(const Args& a, cudaStream_t s) {
     k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
 }
 
+// The hardware approximations of the PTX ISA with subnormal inputs and results
+// flushed to zero (no pair term produces or uses a subnormal value that matters),
+// which spares the instructions that handle subnormals around each one.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_ftz(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+constexpr float kLog2e = 1.4426950408889634f;
+
 // erfc(x) for x >= 0: Abramowitz & Stegun, Handbook of Mathematical Functions,
 // eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term.
 __device__ __forceinline__ float erfc_as(float x, float expmx2) {
-    const float t = __fdividef(1.0f, 1.0f + 0.3275911f * x);
+    const float t = rcp_ftz(1.0f + 0.3275911f * x);
     const float p =
         t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
     return p * expmx2;
@@ -522,7 +543,7 @@ __device__ __forceinline__ float erfc_as(float x, float expmx2) {
 template <int METHOD>
 __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float eps4, float alpha, float krf, float crf,
                                           float& e, float& fr) {
-    const float invr = rsqrtf(r2);
+    const float invr = rsqrt_ftz(r2);
     const float invr2 = invr * invr;
     const float s2 = sig * sig * invr2;
     const float s6 = s2 * s2 * s2;
@@ -530,9 +551,8 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
     e = t6 * s6 - t6;
     fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
     if (METHOD == 4) {
-        const float r = r2 * invr;
-        const float ar = alpha * r;
-        const float ex = __expf(-ar * ar);
+        const float ar = alpha * (r2 * invr);
+        const float ex = ex2_ftz(r2 * (-alpha * alpha * kLog2e));  // exp(-alpha^2 r^2)
         const float ec = erfc_as(ar, ex) * invr;
         e += qq * ec;
         fr += qq * (ec + 1.1283791670955126f * alpha * ex) * invr2;
@@ -610,7 +630,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
         const float r2 = dx * dx + dy * dy + dz * dz;
         const bool inc = ((mask >> k) & 1u) && r2 < rc2;
         const float r2s = inc ? r2 : 1.0f;
-        const float invr = rsqrtf(r2s), invr2 = invr * invr;
+        const float invr = rsqrt_ftz(r2s), invr2 = invr * invr;
         const float sig = li.x + lj.x;
         const float s2 = sig * sig * invr2, s6 = s2 * s2 * s2;
         const float t6 = (li.y * lj.y) * s6;
@@ -620,7 +640,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
         float gq;
         if (METHOD == 4) {
             const float ar = alpha * r2s * invr;
-            const float ex = __expf(-ar * ar);
+            const float ex = ex2_ftz(r2s * (-alpha * alpha * kLog2e));
             gq = erfc_as(ar, ex) * invr;
             fr += pi.w * pj.w * (gq + 1.1283791670955126f * alpha * ex) * invr2;
         } else {
