@@ -590,9 +590,15 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
         const float r2 = dx * dx + dy * dy + dz * dz;
         const bool inc = MASKED ? (((mask >> k) & 1u) && r2 < rc2) : r2 < rc2;
         float e, fr;
-        pair_eval<METHOD>(inc ? r2 : 1.0f, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
-        e = inc ? e : 0.0f;
-        fr = inc ? fr : 0.0f;
+        if (METHOD == 4) {
+            // a pair not counted is evaluated at r^2 = 1e30 nm^2, where every term
+            // comes out exactly zero (r^-6 and exp(-a^2 r^2) underflow; no overflow)
+            pair_eval<METHOD>(inc ? r2 : 1.0e30f, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
+        } else {
+            pair_eval<METHOD>(inc ? r2 : 1.0f, pi.w * pj.w, li.x + lj.x, li.y * lj.y, alpha, krf, crf, e, fr);
+            e = inc ? e : 0.0f;
+            fr = inc ? fr : 0.0f;
+        }
         if (DIFF) e64 += (double)e;
         else e32 += e;
         const float fx = fr * dx, fy = fr * dy, fz = fr * dz;
