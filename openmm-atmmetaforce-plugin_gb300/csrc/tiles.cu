@@ -549,14 +549,17 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
     const float s6 = s2 * s2 * s2;
     const float t6 = eps4 * s6;
     e = t6 * s6 - t6;
-    fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
     if (METHOD == 4) {
-        const float ar = alpha * (r2 * invr);
         const float ex = ex2_ftz(r2 * (-alpha * alpha * kLog2e));  // exp(-alpha^2 r^2)
-        const float ec = erfc_as(ar, ex) * invr;
+        // erfc(alpha r) as in erfc_as, with the constant folded into alpha
+        const float t = rcp_ftz(fmaf(0.3275911f * alpha, r2 * invr, 1.0f));
+        const float ec =
+            t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f)))) *
+            ex * invr;
         e += qq * ec;
-        fr += qq * (ec + 1.1283791670955126f * alpha * ex) * invr2;
+        fr = (12.0f * t6 * s6 - 6.0f * t6 + qq * (ec + 1.1283791670955126f * alpha * ex)) * invr2;
     } else {
+        fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
         e += qq * (invr + krf * r2 - crf);
         fr += qq * (invr * invr2 - 2.0f * krf);
     }
