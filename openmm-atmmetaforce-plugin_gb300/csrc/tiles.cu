@@ -557,7 +557,7 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
             t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f)))) *
             ex * invr;
         e += qq * ec;
-        fr = (12.0f * t6 * s6 - 6.0f * t6 + qq * (ec + 1.1283791670955126f * alpha * ex)) * invr2;
+        fr = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * (ec + 1.1283791670955126f * alpha * ex)) * invr2;
     } else {
         fr = (12.0f * t6 * s6 - 6.0f * t6) * invr2;
         e += qq * (invr + krf * r2 - crf);
@@ -604,13 +604,12 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
         }
         if (DIFF) e64 += (double)e;
         else e32 += e;
-        const float fx = fr * dx, fy = fr * dy, fz = fr * dz;
-        fi.x -= fx;
-        fi.y -= fy;
-        fi.z -= fz;
-        fj.x = __shfl_sync(FULL_MASK, fj.x + fx, src);
-        fj.y = __shfl_sync(FULL_MASK, fj.y + fy, src);
-        fj.z = __shfl_sync(FULL_MASK, fj.z + fz, src);
+        fi.x = fmaf(-fr, dx, fi.x);
+        fi.y = fmaf(-fr, dy, fi.y);
+        fi.z = fmaf(-fr, dz, fi.z);
+        fj.x = __shfl_sync(FULL_MASK, fmaf(fr, dx, fj.x), src);
+        fj.y = __shfl_sync(FULL_MASK, fmaf(fr, dy, fj.y), src);
+        fj.z = __shfl_sync(FULL_MASK, fmaf(fr, dz, fj.z), src);
     }
 }
 
