@@ -29,11 +29,11 @@ METRIC = "ATM evals/sec/replica at 23.5k-atom PME: batched vs plain on one GB300
 F_PAIR = 55.0  # FP32 flops per pair (accounting constant)
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) of one k_tiles launch on this workload, from an ncu
-# --set full capture (92.50 MB read + 6.22 MB write)
-TILES_TRAFFIC_BYTES = 98.71e6
+# --set full capture (92.53 MB read + 6.08 MB write)
+TILES_TRAFFIC_BYTES = 98.62e6
 # warp instructions of one k_tiles launch on this workload (same capture): the
 # kernel is issue-bound, so its issue rate is the second roofline reported
-TILES_WARP_INSTR = 460.4e6
+TILES_WARP_INSTR = 431.7e6
 
 
 def parse():
