@@ -456,7 +456,7 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     const int zword = row | (kind << 28);
     for (int k = lane; k < nblock; k += 32) {
         const int4 e = se[s0 + k];
-        a.tiles[tbase + k] = make_int4(e.x, e.y, zword, (int)((unsigned)(e.z + 1) | ((unsigned)k << 20) | (1u << 31)));
+        a.tiles[tbase + k] = make_int4(e.x, e.y, zword, (int)((unsigned)(e.z + 1) | ((unsigned)k << 20) | (pbc << 31)));
     }
     for (int k = lane; k < nta + ntb; k += 32) {
         const bool hb = k >= nta;
@@ -579,7 +579,7 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
     const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     // the unmasked atom tiles carry most pairs; the other variants stay compact
     // so that the hot loop keeps the instruction cache
-    constexpr int kUnroll = (!PBC && !DIFF && !MASKED) ? 8 : 2;
+    constexpr int kUnroll = (!PBC && !DIFF) ? (MASKED ? 4 : 8) : 2;
 #pragma unroll kUnroll
     for (int k = 0; k < kHalf; k++) {
         const float4 pj = sp[k];
