@@ -46,7 +46,8 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-md", action="store_true", help="skip the MD step-rate measurements")
-    p.add_argument("--md-steps", type=int, default=200)
+    p.add_argument("--md-steps", type=int, default=10000,
+                   help="MD steps of the single 23,558-atom replica (22-replica runs take 1/50, RBFE 1/100)")
     p.add_argument("--tune-cache", action="store_true",
                    help="reuse a stored autotuning choice for this GPU and workload (profiling runs)")
     return p.parse_args()
@@ -165,17 +166,23 @@ def count_pairs(case):
     return n_all - n_exc, n_lig
 
 
-def cpu_baseline(case, threads, evals=2):
+def cpu_baseline(cases, threads, warm=True):
+    """The FP64 oracle timed on the host cores: one full ATM evaluation (two inner
+    evaluations + merge) of each case.  Returns (evals/s, the oracle's results)."""
     import oracle as O
 
     O.set_threads(threads)
-    O.atm_eval(case.spec, case.pos, case.displ, case.params)  # warm
+    if warm:
+        O.atm_eval(cases[0].spec, cases[0].pos, cases[0].displ, cases[0].params)
     t0 = time.perf_counter()
-    for _ in range(evals):
-        O.atm_eval(case.spec, case.pos, case.displ, case.params)
-    dt = (time.perf_counter() - t0) / evals
+    refs = [O.atm_eval(c.spec, c.pos, c.displ, c.params) for c in cases]
+    dt = (time.perf_counter() - t0) / len(cases)
     O.set_threads(1)
-    return 1.0 / dt, dt
+    return 1.0 / dt, refs
+
+
+def force_rms_rel(F, G):
+    return float(np.sqrt(((F - G) ** 2).sum() / (G ** 2).sum()))
 
 
 def reference_arm(args, rank, world, pg):
@@ -211,38 +218,60 @@ def reference_arm(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
-def md_bench(cases_fn, R, steps, warmup, device):
-    """Langevin MD step rate of R replicas stepped together (OpenMM's
-    LangevinIntegrator settings of the reference's ABFE test: 300 K, 0.5/ps,
-    1 fs; rigid water).  Host wall clock around ``step(steps)``, which ends with a
-    device synchronisation; every step is one batched ATM evaluation plus the
-    group-0 terms, the Langevin update, SETTLE and the velocity update."""
+MD_SETTINGS = {"temperature_K": 300.0, "friction_per_ps": 1.0, "step_size_ps": 0.002,
+               "constraints": "rigid water (SETTLE)",
+               "group0": "ligand bonds and angles; flat-bottom restraint of every ligand atom to its ligand's "
+                         "centroid, k 25 kJ/mol/nm^2, tolerance 0.15 nm"}
+
+
+def md_bench(cases_fn, R, steps, warmup, device, record_interval=0):
+    """Langevin MD step rate of R replicas stepped together: 300 K, 1/ps friction,
+    2 fs steps, rigid water, the ligands' bonds and angles and the flat-bottom
+    centroid restraint of every ligand atom.  Host wall clock around
+    ``step(steps)``, which ends with a device synchronisation; every step is one
+    batched ATM evaluation plus the group-0 terms, the Langevin update, SETTLE and
+    the velocity update.  With record_interval, the replicas' result records
+    (u, W, dW/dlambda1, dW/dlambda2, ...) and the R x R reduced-energy matrix are
+    kept on the device every record_interval steps and drained once at the end
+    (inside the timed region)."""
     import atmmetaforce as atm
     from atmmetaforce import synthetic as S
 
     cases, terms = [], []
     for r in range(R):
         c = cases_fn(r)
-        t, p = S.md_terms(c)
+        t, p = S.md_terms_ligand_centroid(c)
         c.pos = p
         cases.append(c)
         terms.append(t)
     systems = [atm.md_system_from_case(c, t)[0] for c, t in zip(cases, terms)]
-    dt = 0.001
-    integ = atm.LangevinIntegrator(300.0, 0.5, dt)
+    dt = MD_SETTINGS["step_size_ps"]
+    integ = atm.LangevinIntegrator(MD_SETTINGS["temperature_K"], MD_SETTINGS["friction_per_ps"], dt)
     integ.setRandomNumberSeed(2024)
     sim = atm.ReplicaSimulation(systems, integ, device)
     sim.setPositions(np.concatenate([c.pos for c in cases]))
-    sim.setVelocitiesToTemperature(300.0, 7)
+    sim.setVelocitiesToTemperature(MD_SETTINGS["temperature_K"], 7)
     sim.step(warmup)
+    if record_interval:
+        sim.setRecording(record_interval, capacity=steps // record_interval + 1)
     t0 = time.perf_counter()
     sim.step(steps)
+    rec = sim.getRecords() if record_interval else None
     el = time.perf_counter() - t0
     sps = steps / el
     n_atoms = int(sum(c.n for c in cases))
+    st = sim.getState(getEnergy=True)
+    temps = sim.temperatures(st.getKineticEnergy())
     out = {"replicas": R, "atoms": n_atoms, "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 * el / steps,
-           "steps_per_s": sps, "step_size_ps": dt, "ns_per_day_per_replica": sps * dt * 86400.0 / 1000.0,
-           "ns_per_day_aggregate": R * sps * dt * 86400.0 / 1000.0, "reorders": sim.info()["reorders"]}
+           "steps_per_s": sps, "ns_per_day_per_replica": sps * dt * 86400.0 / 1000.0,
+           "ns_per_day_aggregate": R * sps * dt * 86400.0 / 1000.0, "reorders": sim.info()["reorders"],
+           "lambdas": [[float(c.params[0]), float(c.params[1])] for c in cases[:1]] if R == 1 else "22-state schedule",
+           "final_temperature_K": float(np.mean(temps)), "settings": MD_SETTINGS}
+    if rec is not None:
+        out["records"] = {"interval_steps": record_interval, "kept": int(len(rec["steps"])),
+                          "per_record": "R result records (u, W, dW/dlambda1, dW/dlambda2, ...) + R x R matrix",
+                          "last_dW_dlambda1": rec["results"][-1, :, 10].tolist()[:3],
+                          "last_dW_dlambda2": rec["results"][-1, :, 11].tolist()[:3]}
     del sim
     return out
 
@@ -261,10 +290,13 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     R = args.replicas
-    cases = []
-    for r in range(R):
-        l1, l2 = S.SCHEDULE_22[r % 22]
-        cases.append(S.abfe_pme_23558(seed=100 + 1000 * rank + r, lambdas=(l1, l2), alpha=0.1, u0=110.0))
+    if R == 22:
+        cases = S.abfe_pme_23558_x22(seed0=100 + 1000 * rank)
+    else:
+        cases = []
+        for r in range(R):
+            l1, l2 = S.SCHEDULE_22[r % 22]
+            cases.append(S.abfe_pme_23558(seed=100 + 1000 * rank + r, lambdas=(l1, l2), alpha=0.1, u0=110.0))
     systems = [atm.system_from_case(c)[0] for c in cases]
     pos_host = np.ascontiguousarray(np.concatenate([c.pos for c in cases]))
     batch = atm.ReplicaBatch(systems, local, {"DifferencePath": 1})
@@ -315,6 +347,7 @@ def main():
     e2e_value = world * R / e2e_s
     h2d = pos_host.nbytes
     d2h = F.nbytes + R * atm.NUM_RES * 8 + R * R * 8  # forces, result records, R x R matrix
+    F_gpu, res_gpu = F.copy(), res.copy()  # the last evaluation of the batch (positions pos_host)
 
     # plain single-replica drop-in (two full inner evaluations)
     plain = None
@@ -329,6 +362,7 @@ def main():
         ms_plain = timed_steps(pb, dp1, df1, dr1, args.steps, args.warmup)
         plain = {"value": 1000.0 / ms_plain, "unit": "evals/s", "ms_per_eval": ms_plain,
                  "config": "1 replica, two full inner evaluations (reference's path)"}
+        _, F_plain, res_plain = pb.evaluate(cases[0].pos, as_array=True)
         pbd = atm.ReplicaBatch([atm.system_from_case(cases[0])[0]], local, {"DifferencePath": 1})
         pbd.evaluate(cases[0].pos)
         pbd.autotune(trials=5, use_cache=args.tune_cache)
@@ -390,20 +424,38 @@ def main():
             c.params = S.default_params(l1, l2, 0.1, 110.0, 0.0, 200.0, 100.0, 0.0625, 1.0)
             return c
 
-        md = {"abfe-pme-23558 x1": md_bench(abfe, 1, 5 * args.md_steps, 20, local),
-              "abfe-pme-23558 x22": md_bench(abfe, 22, args.md_steps, 20, local),
-              "rbfe-pme-60000 x22": md_bench(rbfe, 22, max(20, args.md_steps // 2), 10, local)}
+        def plain_md(r):  # lambda1 = lambda2 = 0.25, alpha 0
+            return S.abfe_pme_23558(seed=100 + 1000 * rank + r)
+
+        md = {"abfe-pme-23558 x1": md_bench(plain_md, 1, args.md_steps, 20, local),
+              "abfe-pme-23558 x22": md_bench(abfe, 22, max(20, args.md_steps // 50), 20, local),
+              "rbfe-pme-60000 x22": md_bench(rbfe, 22, max(20, args.md_steps // 100), 10, local,
+                                             record_interval=1)}
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         threads = os.cpu_count() or 1
-        v, dt = cpu_baseline(cases[0], threads, evals=2)
-        v1, dt1 = cpu_baseline(cases[0], 1, evals=1)
+        checked = sorted({0, R - 1})
+        v, refs = cpu_baseline([cases[k] for k in checked], threads)
+        v1, _ = cpu_baseline([cases[0]], 1, warm=False)
         cpu = {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
-               "sample": "2 evaluations of one 23,558-atom replica (two full FP64 inner evaluations + merge)",
+               "sample": f"{len(checked)} evaluations (replicas {checked}) of the 23,558-atom batch, two full "
+                         "FP64 inner evaluations + merge each",
                "single_thread": {"value": v1, "unit": "evals/s", "cores": 1,
                                  "sample": "1 evaluation, one thread (the serial Reference-platform shape)"}}
+        # the oracle's evaluations double as the checker of the batch's results for those replicas
+        pert = atm.RES_KEYS.index("pert")
+        du, fr = [], []
+        for k, ref in zip(checked, refs):
+            du.append(abs(float(res_gpu[k, pert]) - ref["usc"]))
+            fr.append(force_rms_rel(F_gpu[batch.offsets[k]:batch.offsets[k + 1]], ref["forces"]))
+        parity = {"replicas_checked": checked, "max_du_kj_mol": max(du), "max_force_rms_rel": max(fr),
+                  "targets": {"du_kj_mol": 0.01, "force_rms_rel": 1e-4}, "oracle": "FP64 CPU restatement"}
+        if plain is not None:
+            parity["plain_replica0"] = {"du_kj_mol": abs(float(res_plain[0, pert]) - refs[0]["usc"]),
+                                        "force_rms_rel": force_rms_rel(F_plain, refs[0]["forces"])}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -421,7 +473,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": batch.launchCount() * args.steps,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(), "md": md}
+                "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "md": md}
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()

@@ -10,7 +10,7 @@
  * Object model (mirrors OpenMM's, which the reference plugs into):
  *   atm_force_t      ATMMetaForce                   openmmapi/include/ATMMetaForce.h:54-315
  *   atm_nonbonded_t  the inner NonbondedForce the ATM force re-evaluates
- *                    (ATMMetaForceImpl.cpp:96-110 clones it into the inner systems)
+ *                    (ATMMetaForceImpl.cpp:32-67 clones it into the inner systems)
  *   atm_system_t     System: particles, default box, forces (owned, as in OpenMM)
  *   atm_context_t    one evaluation context on one GPU (ATMMetaForceImpl +
  *                    CalcATMMetaForceKernel, ATMMetaForceKernels.h:15-59)
@@ -117,7 +117,7 @@ int atm_force_get_name(atm_force_t force, char* buf, size_t cap, size_t* len);
 int atm_force_uses_periodic_boundary_conditions(atm_force_t force, int* uses);
 /* updateParametersInContext, ATMMetaForce.h:130 / CommonATMMetaForceKernels.cpp:229-251. */
 int atm_force_update_parameters_in_context(atm_force_t force, atm_context_t context);
-/* getPerturbationEnergy, ATMMetaForce.h:145 / ATMMetaForceImpl.cpp:125. */
+/* getPerturbationEnergy, ATMMetaForce.h:145 / ATMMetaForceImpl.cpp:124-125. */
 int atm_force_get_perturbation_energy(atm_force_t force, atm_context_t context, double* value);
 /* XmlSerializer::serialize<ATMMetaForce> through ATMMetaForceProxy::serialize,
  * serialization/src/ATMMetaForceProxy.cpp:11-40.  Writes a NUL-terminated
@@ -126,7 +126,7 @@ int atm_force_serialize(atm_force_t force, char* buf, size_t cap, size_t* len);
 /* ATMMetaForceProxy::deserialize, ATMMetaForceProxy.cpp:42-79. */
 int atm_force_deserialize(const char* xml, atm_force_t* out);
 
-/* ---- inner NonbondedForce (OpenMM NonbondedForce, cloned by ATMMetaForceImpl.cpp:103-108) -- */
+/* ---- inner NonbondedForce (OpenMM NonbondedForce, cloned by ATMMetaForceImpl.cpp:58-63) --- */
 int atm_nonbonded_create(atm_nonbonded_t* out);
 int atm_nonbonded_destroy(atm_nonbonded_t nb);
 int atm_nonbonded_add_particle(atm_nonbonded_t nb, double charge, double sigma, double epsilon, int* index);
@@ -188,13 +188,15 @@ int atm_context_destroy(atm_context_t ctx);
 /* Context::setPositions (host doubles, n x 3, nm). */
 int atm_context_set_positions(atm_context_t ctx, const double* pos, int n);
 int atm_context_set_periodic_box_vectors(atm_context_t ctx, const double* a, const double* b, const double* c);
-/* Context::setParameter / getParameter for the ATM globals (ATMMetaForceImpl.cpp:175-187). */
+/* Context::setParameter / getParameter for the ATM globals, which the force
+ * registers as context parameters with their defaults (ATMMetaForceImpl.cpp:130-142). */
 int atm_context_set_parameter(atm_context_t ctx, const char* name, double value);
 int atm_context_get_parameter(atm_context_t ctx, const char* name, double* value);
 /* Context::getState(getEnergy, getForces, groups): energy and forces (n x 3,
  * host, nullable) of the forces whose group bit is set in groups_mask
- * (ATMMetaForceImpl.cpp:135-173: the ATM force contributes only when its group
- * is requested; its forces are merged even if forces are not requested). */
+ * (ATMMetaForceImpl.cpp:103: the ATM force contributes only when its group
+ * is requested; :113,116,119-122: its forces are merged even if forces are not
+ * requested). */
 int atm_context_get_state(atm_context_t ctx, int groups_mask, double* energy, double* forces);
 /* Last per-replica result record (ATM_NUM_RES doubles). */
 int atm_context_get_results(atm_context_t ctx, double* results);

@@ -409,3 +409,21 @@ def md_terms(case, n_receptor=8, bond_k=2.5e5, angle_k=500.0, rigid_water=True):
                     posres_ref=pos.copy(), posres_fc=25.0 * KCAL_A2, posres_tol=0.05, posres_periodic=True,
                     centroid=centroid)
     return terms, pos
+
+
+def md_terms_ligand_centroid(case, kf=25.0, tol=0.15, bond_k=2.5e5, angle_k=500.0, rigid_water=True):
+    """MD terms of the benchmark's plain-ATM MD runs: masses, rigid waters, each
+    ligand's bonds and angles at their built geometry, and a flat-bottom harmonic
+    restraint of every ligand atom to its ligand's mass-weighted centroid,
+    (kf/2) step(d - tol)(d - tol)^2 with d = |x_i - c_ligand| (kf in kJ/mol/nm^2,
+    tol in nm; each one a centroid restraint of the atom against its ligand, no
+    periodic image).  No receptor, so no position restraints.  Returns (terms,
+    positions)."""
+    terms, pos = md_terms(case, n_receptor=0, bond_k=bond_k, angle_k=angle_k, rigid_water=rigid_water)
+    cent = []
+    for lig in case.ligands:
+        g2 = np.asarray(lig, dtype=int)
+        for i in g2:
+            cent.append((np.array([int(i)]), g2, float(kf), float(tol), np.zeros(3)))
+    terms.centroid = cent
+    return terms, pos

@@ -642,7 +642,7 @@ int atm_context_get_state(atm_context_t ctx, int groups_mask, double* energy, do
         ctx->eng->evaluate(nullptr, ctx->forces.data(), ctx->forces_nb.data(), ctx->results.data(), nullptr);
         ctx->dirty = false;
     }
-    // ATMMetaForceImpl.cpp:148,169-172: the perturbation energy is refreshed when the ATM group is evaluated
+    // ATMMetaForceImpl.cpp:103,125: the perturbation energy is refreshed only when the ATM group is evaluated
     if (want_atm) ctx->pert = ctx->results[RES_PERT];
     double e = 0.0;
     if (want_atm) e += ctx->results[RES_ENERGY];

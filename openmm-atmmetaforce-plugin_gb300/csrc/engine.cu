@@ -2,7 +2,7 @@
 // the CUDA graph that runs one ATM evaluation of all replicas.
 //
 // Reference correspondence: the engine replaces ATMMetaForceImpl's two linked
-// inner contexts (ATMMetaForceImpl.cpp:135-173) and CommonCalcATMMetaForceKernel
+// inner contexts (ATMMetaForceImpl.cpp:32-67,94-95) and CommonCalcATMMetaForceKernel
 // (CommonATMMetaForceKernels.cpp:78-251): CopyState becomes the displacement of
 // the state-2 slots (k_prepare), the two inner evaluations become one pass over
 // both states (or over state 1 plus the ligand difference), and execute() runs
@@ -48,7 +48,7 @@ ReplicaSpec spec_from_system(const System& sys) {
     if ((int)nb.charge.size() != n) throw Error(1, "NonbondedForce particle count differs from the System's");
     if (f.getNumParticles() != n)
         throw Error(9, "ATMMetaForce must hold every System particle (ATMMetaForce.h:94-104)");
-    // ATMMetaForceImpl.cpp:120-126
+    // ATMMetaForceImpl.cpp:75-81
     for (int g : f.groups) {
         if (g == f.forceGroup) throw Error(8, "The ATM Meta Force group cannot be one of the variable force groups.");
         if (g < 0 || g > 31) throw Error(1, "Variable force groups must be between 0 and 31");

@@ -29,7 +29,7 @@ struct ReplicaSpec {
 };
 
 // Build a ReplicaSpec from a System holding one NonbondedForce and one
-// ATMMetaForce (the inner-system copy of ATMMetaForceImpl.cpp:77-112).
+// ATMMetaForce (the inner-system copy of ATMMetaForceImpl.cpp:32-67).
 ReplicaSpec spec_from_system(const System& sys);
 
 struct KernelTime {

@@ -609,7 +609,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(Args a) {
     const float vol = R.box[0] * R.box[1] * R.box[2];
     const float pref = 1.0f / (pi * vol);
     const float fac = pi * pi / (a.alpha * a.alpha);
-    float ea = 0.f, eb = 0.f;
+    // the reciprocal energies (and with them u) accumulate in FP64; each point's
+    // term is an FP32 product
+    double ea = 0.0, eb = 0.0;
     for (long long k = first + threadIdx.x; k < last; k += kConvThreads) {
         int iz = (int)(k % Kzh);
         long long rem = k / Kzh;
@@ -623,11 +625,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(Args a) {
         float wgt = (iz == 0 || 2 * iz == Kz) ? 1.0f : 2.0f;
         float2 qa = A[k], qb = B[k];
         float na = qa.x * qa.x + qa.y * qa.y;
-        ea += 0.5f * wgt * G * na;
+        ea += (double)(0.5f * wgt * G * na);
         if (a.full) {
-            eb += 0.5f * wgt * G * (qb.x * qb.x + qb.y * qb.y);
+            eb += (double)(0.5f * wgt * G * (qb.x * qb.x + qb.y * qb.y));
         } else {
-            eb += wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y));
+            eb += (double)(wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y)));
         }
         A[k] = make_float2(G * qa.x, G * qa.y);
         B[k] = make_float2(G * qb.x, G * qb.y);

@@ -806,19 +806,14 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         }
         __syncwarp();
         const bool diag = !atom_tile && T.y == I16;
-        // tile energy over the half: FP64 on the difference tiles (their sum is u),
-        // FP32 otherwise (FP64 arithmetic is scarce on this part); fixed order either way
-        double esum;
-        if (diff) {
-            esum = e64;
+        // tile energy over the half, in FP64 and a fixed order: the difference tiles
+        // sum every pair term in FP64 (their sum is u); the state tiles keep one FP32
+        // partial of 16 pair terms per lane (FP64 arithmetic is scarce on this part)
+        // and sum the partials in FP64, so that u = E2 - E1 of the two-state mode is a
+        // difference of FP64 sums
+        double esum = diff ? e64 : (double)(diag ? 0.5f * e32 : e32);
 #pragma unroll
-            for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
-        } else {
-            float es = diag ? 0.5f * e32 : e32;
-#pragma unroll
-            for (int o = kHalf / 2; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
-            esum = (double)es;
-        }
+        for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
         const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
         if (l == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
         if (!atom_tile || aux > 0) {  // (an empty tile, the filler of an odd row, adds nothing)

@@ -12,9 +12,11 @@ Amber prmtop and equilibrated OpenMM state XML:
   (nm), epsilon (kJ/mol), the guest's atom indices, and the exception list
   (1-2/1-3 exclusions, scaled 1-4 pairs).
 
-Run from the repository root:  python tests/golden/make_temoa_fixture.py
-(reads the reference checkout; the fixture it writes is committed, so tests do
-not need the reference at run time).
+Run from the repository root with the reference checkout named explicitly:
+  ATM_REFERENCE_DIR=<reference checkout> python tests/golden/make_temoa_fixture.py
+or  python tests/golden/make_temoa_fixture.py <reference checkout> [out.npz]
+(the fixture it writes is committed, so tests do not need the reference at run
+time).
 """
 from __future__ import annotations
 
@@ -23,8 +25,6 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("ATM_REFERENCE_DIR", "/root/reference")
-SRC = os.path.join(REF, "python", "tests")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "temoa_g1.npz")
 
 KCAL = 4.184
@@ -34,12 +34,13 @@ sys.path.insert(0, os.path.join(ROOT, "openmm-atmmetaforce-plugin_gb300"))
 from atmmetaforce.amber import read_prmtop, read_state_xml  # noqa: E402
 
 
-def main(out=OUT):
-    prm = read_prmtop(os.path.join(SRC, "temoa-g1.prmtop"))
+def main(ref, out=OUT):
+    src = os.path.join(ref, "python", "tests")
+    prm = read_prmtop(os.path.join(src, "temoa-g1.prmtop"))
     natom = prm.natom
     # residues: the guest is residue 2 (1-based), as test_abfe.py:26,47-50 selects it
     ligand = prm.residue_atoms(1)
-    pos, box = read_state_xml(os.path.join(SRC, "temoa-g1-equil.xml"))
+    pos, box = read_state_xml(os.path.join(src, "temoa-g1-equil.xml"))
     assert pos.shape == (natom, 3), pos.shape
     charge, sigma, epsilon, box_default = prm.charge, prm.sigma, prm.epsilon, prm.box
     ei, ej, eqq, esig, eeps = prm.exc_i, prm.exc_j, prm.exc_qq, prm.exc_sig, prm.exc_eps
@@ -61,4 +62,7 @@ def main(out=OUT):
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else OUT))
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ATM_REFERENCE_DIR")
+    if not ref:
+        sys.exit("name the reference checkout: ATM_REFERENCE_DIR=<dir> or the first argument")
+    sys.exit(main(ref, sys.argv[2] if len(sys.argv) > 2 else OUT))

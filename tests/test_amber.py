@@ -111,10 +111,11 @@ def _fixture_script():
 
 def test_reader_reproduces_the_committed_temoa_fixture(tmp_path):
     mod = _fixture_script()
-    if not os.path.exists(os.path.join(mod.SRC, "temoa-g1.prmtop")):
-        pytest.skip("the reference checkout the fixture was made from is absent")
+    ref = os.environ.get("ATM_REFERENCE_DIR")
+    if not ref or not os.path.exists(os.path.join(ref, "python", "tests", "temoa-g1.prmtop")):
+        pytest.skip("ATM_REFERENCE_DIR does not name the reference checkout the fixture was made from")
     out = tmp_path / "temoa.npz"
-    mod.main(str(out))
+    mod.main(ref, str(out))
     here = os.path.dirname(os.path.abspath(__file__))
     a = np.load(os.path.join(here, "golden", "temoa_g1.npz"))
     b = np.load(out)

@@ -118,7 +118,7 @@ def test_particle_index_errors():
 
 
 def test_context_rejects_atm_group_among_variable_groups():
-    # ATMMetaForceImpl.cpp:122-124, checked before any device work
+    # ATMMetaForceImpl.cpp:75-81, checked before any device work
     c = S.water_ligand_box(300, 2.0, [4], [(1.0, 1.0, 1.0)], S.PME, 0.9, seed=1)
     sys_, nb, f = atm.system_from_case(c, nonbonded_group=1, atm_group=1)
     with pytest.raises(atm.ATMError) as e:

@@ -4,7 +4,10 @@ Checks dW/d(positions), dW/d(displacement), dW/d(ligand q, sigma, eps) and the
 five softplus parameters against (a) the oracle's analytic gradient and
 (b) central finite differences of W computed in FP64 (h = 1e-4; the pair set
 is frozen at the unperturbed geometry so that the plain cutoff does not make
-W jump).  Tolerance: 1e-3 relative.
+W jump).  Tolerance: 1e-3 relative, with no absolute floor; the finite
+differences are taken on the components where the analytic gradient is largest.
+Cases: two 3,000-atom boxes (directions +1 and -1), and the batch of eight
+12,000-atom PME boxes with 30-atom ligands displaced by (2,2,2) nm.
 """
 import copy
 import os
@@ -96,36 +99,45 @@ def test_adjoint_matches_analytic_oracle_gradient(setup):
         assert rel_err(grads["params"][k], ref["params"]) <= REL
 
 
-def test_adjoint_matches_finite_differences(setup):
-    cases, b, res, grads = setup
-    c = cases[0]
-    a = b.offsets[0]
+def _top(v, k):
+    """Indices of the k entries of v largest in magnitude."""
+    return np.argsort(-np.abs(np.asarray(v).ravel()), kind="stable")[:k]
+
+
+def fd_check(c, grads, k, a, ref, n_pos=6, n_displ=4, n_param_atoms=2):
+    """Central differences of W (FP64 oracle, h = 1e-4, pair set frozen at the
+    unperturbed geometry) against the GPU adjoint of replica k (atoms from offset
+    a), on the components where the analytic gradient is largest: a relative
+    bound is only meaningful away from zero.  Returns the largest relative error."""
+    worst = 0.0
     lig = c.ligands[0]
-    rng = np.random.default_rng(1)
-    # positions: two ligand coordinates and two water coordinates near the ligand
-    env = np.argsort(((c.pos - c.pos[lig].mean(0)) ** 2).sum(1))[len(lig) + 3:len(lig) + 5]
-    for i in list(lig[:2]) + list(env):
-        for d in range(3):
-            p1, p2 = c.pos.copy(), c.pos.copy()
-            p1[i, d] += H
-            p2[i, d] -= H
-            fd = (W_of(c.spec, p1, c.displ, c.params, c.pos, c.displ) -
-                  W_of(c.spec, p2, c.displ, c.params, c.pos, c.displ)) / (2 * H)
-            got = grads["positions"][a + i, d]
-            assert abs(got - fd) <= REL * max(abs(fd), 1.0) + 1e-3, (i, d, got, fd)
-    # displacement of a ligand atom
-    for i in lig[:3]:
-        for d in range(3):
-            d1, d2 = c.displ.copy(), c.displ.copy()
-            d1[i, d] += H
-            d2[i, d] -= H
-            fd = (W_of(c.spec, c.pos, d1, c.params, c.pos, c.displ) -
-                  W_of(c.spec, c.pos, d2, c.params, c.pos, c.displ)) / (2 * H)
-            got = grads["displacements"][a + i, d]
-            assert abs(got - fd) <= REL * max(abs(fd), 1.0) + 1e-3, (i, d, got, fd)
-    # ligand charge, sigma, epsilon
-    for i in lig[[0, 5, 9]]:
-        for key in ("charge", "sigma", "epsilon"):
+
+    def check(got, fd, what):
+        nonlocal worst
+        err = abs(got - fd) / abs(fd)
+        worst = max(worst, err)
+        assert err <= REL, (what, got, fd)
+
+    for flat in _top(ref["positions"], n_pos):
+        i, d = divmod(int(flat), 3)
+        p1, p2 = c.pos.copy(), c.pos.copy()
+        p1[i, d] += H
+        p2[i, d] -= H
+        fd = (W_of(c.spec, p1, c.displ, c.params, c.pos, c.displ) -
+              W_of(c.spec, p2, c.displ, c.params, c.pos, c.displ)) / (2 * H)
+        check(grads["positions"][a + i, d], fd, ("position", i, d))
+    for flat in _top(ref["displacements"][lig], n_displ):
+        m, d = divmod(int(flat), 3)
+        i = int(lig[m])
+        d1, d2 = c.displ.copy(), c.displ.copy()
+        d1[i, d] += H
+        d2[i, d] -= H
+        fd = (W_of(c.spec, c.pos, d1, c.params, c.pos, c.displ) -
+              W_of(c.spec, c.pos, d2, c.params, c.pos, c.displ)) / (2 * H)
+        check(grads["displacements"][a + i, d], fd, ("displacement", i, d))
+    for key in ("charge", "sigma", "epsilon"):
+        for m in _top(ref[key][lig], n_param_atoms):
+            i = int(lig[m])
             s1, s2 = copy.copy(c.spec), copy.copy(c.spec)
             v1 = getattr(c.spec, key).copy()
             v2 = v1.copy()
@@ -135,15 +147,59 @@ def test_adjoint_matches_finite_differences(setup):
             setattr(s2, key, v2)
             fd = (W_of(s1, c.pos, c.displ, c.params, c.pos, c.displ) -
                   W_of(s2, c.pos, c.displ, c.params, c.pos, c.displ)) / (2 * H)
-            got = grads[key][a + i]
-            assert abs(got - fd) <= REL * max(abs(fd), 1.0) + 1e-3, (key, i, got, fd)
-    # the five softplus parameters
-    for k in range(5):
+            check(grads[key][a + i], fd, (key, i))
+    for p in range(5):
         q1, q2 = c.params.copy(), c.params.copy()
-        q1[k] += H
-        q2[k] -= H
-        fd = (W_of(c.spec, c.pos, c.displ, q1, c.pos, c.displ) - W_of(c.spec, c.pos, c.displ, q2, c.pos, c.displ)) / (2 * H)
-        assert abs(grads["params"][0, k] - fd) <= REL * max(abs(fd), 1.0), (k, grads["params"][0, k], fd)
+        q1[p] += H
+        q2[p] -= H
+        fd = (W_of(c.spec, c.pos, c.displ, q1, c.pos, c.displ) -
+              W_of(c.spec, c.pos, c.displ, q2, c.pos, c.displ)) / (2 * H)
+        check(grads["params"][k, p], fd, ("param", p))
+    return worst
+
+
+def test_adjoint_matches_finite_differences(setup):
+    cases, b, res, grads = setup
+    for k in (0, 1):
+        fd_check(cases[k], grads, k, b.offsets[k], oracle_grads(cases[k]))
+
+
+@pytest.fixture(scope="module")
+def batch8():
+    """8 seeded 12,000-atom PME boxes, 30-atom ligands displaced by (2,2,2) nm,
+    softplus parameters lambda U[0,0.5], alpha U[0,0.2], u0 U[50,150]."""
+    O.set_threads(min(16, os.cpu_count() or 1))
+    cases = S.adjoint_batch_8()
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0, {"DifferencePath": 1, "Adjoint": 1})
+    E, F, res = b.evaluate(np.concatenate([c.pos for c in cases]))
+    grads = b.backward()
+    yield cases, b, res, grads
+    O.set_threads(1)
+
+
+def test_adjoint_batch_of_eight_12000_atom_boxes_analytic(batch8):
+    cases, b, res, grads = batch8
+    worst = 0.0
+    for k, c in enumerate(cases):
+        ref = oracle_grads(c)
+        a, z = b.offsets[k], b.offsets[k + 1]
+        assert res[k]["status"] == 0
+        lig = c.ligands[0]
+        errs = [rel_err(grads["positions"][a:z], ref["positions"]),
+                rel_err(grads["displacements"][a:z], ref["displacements"]),
+                rel_err(grads["params"][k], ref["params"])]
+        errs += [rel_err(grads[key][a:z][lig], ref[key][lig]) for key in ("charge", "sigma", "epsilon")]
+        worst = max(worst, max(errs))
+        assert max(errs) <= REL, (k, errs)
+    print(f"8 x 12,000 adjoint: largest relative error against the analytic oracle gradient {worst:.2e}")
+
+
+def test_adjoint_batch_of_eight_12000_atom_boxes_finite_differences(batch8):
+    cases, b, res, grads = batch8
+    worst = 0.0
+    for k in (0, 7):
+        worst = max(worst, fd_check(cases[k], grads, k, b.offsets[k], oracle_grads(cases[k])))
+    print(f"8 x 12,000 adjoint: largest relative error against central differences {worst:.2e}")
 
 
 def test_torch_autograd_function_wires_the_adjoint(setup):

@@ -231,7 +231,7 @@ def test_group_semantics_and_nonbonded_group():
     E1, F1, _ = O.nonbonded(c.spec, c.pos)
     assert abs(s1.getPotentialEnergy() - E1) <= energy_tol(c.spec, c.pos)
     assert force_rel(s1.getForces(), F1) <= F_TOL
-    # the ATM group not requested: perturbation energy not refreshed (ATMMetaForceImpl.cpp:148)
+    # the ATM group not requested: perturbation energy not refreshed (ATMMetaForceImpl.cpp:103,125)
     assert f.getPerturbationEnergy(ctx) == 0.0
     ctx.getState(getEnergy=True, groups={2})
     assert f.getPerturbationEnergy(ctx) != 0.0
