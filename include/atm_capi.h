@@ -182,7 +182,10 @@ int atm_system_set_position_restraints_periodic(atm_system_t sys, int periodic);
 
 /* ---- Context: one replica on one GPU -------------------------------------- */
 /* properties: "key=value;key=value".  Keys: DifferencePath=0|1 (default 0, two
- * full inner evaluations as in ATMMetaForceImpl.cpp:113,116). */
+ * full inner evaluations as in ATMMetaForceImpl.cpp:113,116); ListSkin=nm
+ * (default 0: the pair lists are built at every evaluation; > 0: built at the
+ * cutoff plus the skin and kept until an atom has moved more than half the skin,
+ * which the GPU checks at every evaluation). */
 int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out);
 int atm_context_destroy(atm_context_t ctx);
 /* Context::setPositions (host doubles, n x 3, nm). */
@@ -223,6 +226,9 @@ int atm_batch_evaluate_device(atm_batch_t b, const double* d_pos_all, double* d_
 /* R x R matrix of beta * (e0_r + W_s(u_r)): replica r's coordinates under
  * replica s's alchemical parameters, from the last evaluation. */
 int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix);
+/* No counterpart in the reference.  The list skin, and how many evaluations ran
+ * and how many of them built the pair lists (nullable outputs). */
+int atm_batch_get_list_info(atm_batch_t b, double* skin, long long* evaluations, long long* builds);
 /* Per-replica displacement vectors (n x 3), as ATMMetaForce::setParticleParameters
  * + updateParametersInContext (ATMMetaForce.cpp:26-40) for a batch replica. */
 int atm_batch_set_displacements(atm_batch_t b, int replica, const double* displ);
@@ -249,12 +255,26 @@ int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, d
  * (python/tests/test_abfe.py:96-103, example/abfe/abfe.py:94-101).  systems as
  * for atm_batch_create, plus masses (mass 0: the particle does not move).
  * properties: DifferencePath=0|1 (default 1), ReorderInterval=steps (default
- * 0: re-sort when the pair-tile count has grown by 20 %).  temperature K,
- * friction 1/ps, step_size ps; seed keys the Philox4x32-10 thermostat noise. */
+ * 0: re-sort when the pair-tile count has grown by 20 %), ListSkin=nm|auto
+ * (default 0.1, reduced to what the boxes allow; auto: chosen by
+ * atm_md_autotune before the first step),
+ * CheckInterval=steps (default 20: the host reads the list status every that
+ * many steps instead of after every step, and redoes the steps since the last
+ * check if a list build overflowed).  temperature K, friction 1/ps, step_size
+ * ps; seed keys the Philox4x32-10 thermostat noise. */
 typedef struct atm_md_s* atm_md_t;
 int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
                   double temperature, double friction, double step_size, unsigned long long seed, atm_md_t* out);
 int atm_md_destroy(atm_md_t md);
+/* No counterpart in the reference.  Times the evaluation's launch space, then
+ * `trials` steps at each pair-list skin from 0 to 0.2 nm, keeps the fastest and
+ * writes a report (NUL-terminated, at most cap bytes; *len = bytes needed).  The
+ * positions, velocities, step count and recording are restored afterwards. */
+int atm_md_autotune(atm_md_t md, int trials, char* report, size_t cap, size_t* len);
+/* No counterpart in the reference.  The list skin in use, how many evaluations
+ * ran, how many of them built the pair lists, and how many list checks sent the
+ * state back to their snapshot (nullable outputs). */
+int atm_md_get_list_info(atm_md_t md, double* skin, long long* evaluations, long long* builds, int* redos);
 int atm_md_get_num_particles(atm_md_t md, int* n_total);
 /* Positions / velocities of every replica back to back (host, n_total x 3). */
 int atm_md_set_positions(atm_md_t md, const double* pos);

@@ -105,6 +105,9 @@ _SIGS = {
     "atm_batch_evaluate": [_vp, _dp, _dp, _dp, _dp],
     "atm_batch_evaluate_device": [_vp, _vp, _vp, _vp, _vp],
     "atm_batch_energy_matrix": [_vp, C.c_double, _dp],
+    "atm_batch_get_list_info": [_vp, _dp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
+    "atm_md_autotune": [_vp, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)],
+    "atm_md_get_list_info": [_vp, _dp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _ip],
     "atm_batch_set_displacements": [_vp, C.c_int, _dp],
     "atm_batch_set_nonbonded_parameters": [_vp, C.c_int, _dp, _dp, _dp],
     "atm_batch_backward_device": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],

@@ -557,6 +557,12 @@ class ReplicaBatch:
         call("atm_batch_get_launch_count", self._h, C.byref(n))
         return n.value
 
+    def listInfo(self):
+        """The pair-list skin (nm), the evaluations run and how many built the lists."""
+        skin, ev, bu = C.c_double(), C.c_longlong(), C.c_longlong()
+        call("atm_batch_get_list_info", self._h, C.byref(skin), C.byref(ev), C.byref(bu))
+        return {"skin": skin.value, "evaluations": ev.value, "builds": bu.value}
+
     def stats(self):
         """Pair tiles of the last evaluation, tile rows and the largest row."""
         t, r, m = C.c_int(), C.c_int(), C.c_int()

@@ -282,6 +282,22 @@ class ReplicaSimulation:
         k = n.value
         return {"steps": steps[:k], "results": res[:k], "matrices": mat[:k]}
 
+    def autotune(self, trials=20):
+        """Time the evaluation's launch space and `trials` steps at each pair-list
+        skin (0 to 0.2 nm), keep the fastest; returns the report.  The state is
+        restored afterwards."""
+        buf = C.create_string_buffer(16384)
+        n = C.c_size_t()
+        call("atm_md_autotune", self._h, int(trials), buf, 16384, C.byref(n))
+        return buf.value.decode()
+
+    def listInfo(self):
+        """The pair-list skin (nm), the evaluations run, how many built the lists,
+        and how many list checks sent the state back to their snapshot."""
+        skin, ev, bu, rd = C.c_double(), C.c_longlong(), C.c_longlong(), C.c_int()
+        call("atm_md_get_list_info", self._h, C.byref(skin), C.byref(ev), C.byref(bu), C.byref(rd))
+        return {"skin": skin.value, "evaluations": ev.value, "builds": bu.value, "redos": rd.value}
+
     def info(self):
         steps, reorders = C.c_longlong(), C.c_int()
         dof = (C.c_int * self.R)()

@@ -108,6 +108,18 @@ static bool prop_bool(const std::map<std::string, std::string>& m, const char* k
     throw Error(ATM_ERR_INVALID_ARGUMENT, std::string("Bad value for property ") + key + ": " + v);
 }
 
+static double prop_double(const std::map<std::string, std::string>& m, const char* key, double def) {
+    auto it = m.find(key);
+    if (it == m.end()) return def;
+    try {
+        size_t used = 0;
+        double v = std::stod(it->second, &used);
+        if (used == it->second.size()) return v;
+    } catch (...) {
+    }
+    throw Error(ATM_ERR_INVALID_ARGUMENT, std::string("Bad value for property ") + key + ": " + it->second);
+}
+
 extern "C" {
 
 const char* atm_last_error(void) { return g_error.c_str(); }
@@ -580,6 +592,7 @@ int atm_context_create(atm_system_t sys, int device, const char* properties, atm
     std::vector<ReplicaSpec> v;
     v.push_back(std::move(spec));
     c->eng.reset(new Engine(std::move(v), device, !diff));
+    c->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     c->forces.resize(3 * (size_t)c->n);
     c->forces_nb.resize(3 * (size_t)c->n);
     c->results.resize(NUM_RES);
@@ -678,6 +691,7 @@ int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, co
     }
     std::unique_ptr<atm_batch_s> b(new atm_batch_s);
     b->eng.reset(new Engine(std::move(v), device, !diff, adjoint));
+    b->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     b->results.resize((size_t)NUM_RES * n_replicas);
     b->matrix.resize((size_t)n_replicas * n_replicas);
     *out = b.release();
@@ -811,6 +825,14 @@ int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, d
     API_END
 }
 
+int atm_batch_get_list_info(atm_batch_t b, double* skin, long long* evaluations, long long* builds) {
+    API_BEGIN
+    REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
+    if (skin) *skin = b->eng->list_skin();
+    b->eng->list_counts(evaluations, builds);
+    API_END
+}
+
 int atm_batch_energy_matrix(atm_batch_t b, double beta, double* matrix) {
     API_BEGIN
     REQUIRE(b && matrix, ATM_ERR_INVALID_ARGUMENT, "null argument");
@@ -881,6 +903,19 @@ int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const
     opt.seed = seed;
     auto it = props.find("ReorderInterval");
     if (it != props.end()) opt.reorder_interval = std::stoi(it->second);
+    it = props.find("ListSkin");
+    if (it != props.end()) {
+        if (it->second == "auto") {
+            opt.list_skin = -1.0;
+        } else {
+            opt.list_skin = prop_double(props, "ListSkin", 0.1);
+            REQUIRE(opt.list_skin >= 0.0, ATM_ERR_INVALID_ARGUMENT, "ListSkin must be a non-negative length or auto");
+        }
+    }
+    it = props.find("CheckInterval");
+    if (it != props.end()) opt.check_interval = std::stoi(it->second);
+    it = props.find("TestFailListCheck");
+    if (it != props.end()) opt.fail_check = std::stoi(it->second);
     std::vector<const System*> v;
     for (int r = 0; r < n_replicas; r++) {
         REQUIRE(systems[r], ATM_ERR_INVALID_ARGUMENT, "null system");
@@ -895,6 +930,23 @@ int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const
 int atm_md_destroy(atm_md_t md) {
     API_BEGIN
     delete md;
+    API_END
+}
+
+int atm_md_autotune(atm_md_t md, int trials, char* report, size_t cap, size_t* len) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null simulation");
+    std::string rep = md->md->autotune(trials);
+    copy_string(rep, report, cap, len);
+    API_END
+}
+
+int atm_md_get_list_info(atm_md_t md, double* skin, long long* evaluations, long long* builds, int* redos) {
+    API_BEGIN
+    REQUIRE(md, ATM_ERR_INVALID_ARGUMENT, "null simulation");
+    if (skin) *skin = md->md->engine().list_skin();
+    if (redos) *redos = md->md->redos();
+    md->md->engine().list_counts(evaluations, builds);
     API_END
 }
 

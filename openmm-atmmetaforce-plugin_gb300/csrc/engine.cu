@@ -15,6 +15,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <numeric>
 #include <set>
@@ -166,17 +167,20 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     const ReplicaSpec& s0 = specs_[0];
     method_ = s0.method;
     cutoff_ = s0.cutoff;
-    if (method_ != NonbondedForce::CutoffPeriodic && method_ != NonbondedForce::PME)
-        throw Error(5, "Only CutoffPeriodic (reaction field) and PME nonbonded methods run on the GPU path");
+    if (method_ < NonbondedForce::NoCutoff || method_ > NonbondedForce::PME)
+        throw Error(5, "Unknown nonbonded method");
+    if (method_ == 3) throw Error(5, "Plain Ewald summation is not implemented on the GPU path; use PME");
+    periodic_ = method_ == NonbondedForce::CutoffPeriodic || method_ == NonbondedForce::PME;
     in_off_.resize(R_);
     for (int r = 0; r < R_; r++) {
         const ReplicaSpec& s = specs_[r];
         if (s.n <= 0) throw Error(1, "Empty replica");
         if (s.method != method_ || s.cutoff != cutoff_ || s.epsRF != s0.epsRF || s.alpha != s0.alpha)
             throw Error(5, "All replicas of a batch must share the nonbonded method, cutoff and Ewald parameters");
-        for (int a = 0; a < 3; a++)
-            if (!(s.box[a] >= 2.0 * s.cutoff))
-                throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
+        if (periodic_)
+            for (int a = 0; a < 3; a++)
+                if (!(s.box[a] >= 2.0 * s.cutoff))
+                    throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
         if (s.method == NonbondedForce::PME)
             for (int a = 0; a < 3; a++)
                 if (s.grid[a] < 6) throw Error(1, "PME grid dimensions must be at least 6");
@@ -188,8 +192,12 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     }
     alpha_ = s0.alpha;
     double er = s0.epsRF;
-    krf_ = (er - 1.0) / ((2.0 * er + 1.0) * cutoff_ * cutoff_ * cutoff_);
-    crf_ = 3.0 * er / ((2.0 * er + 1.0) * cutoff_);
+    if (method_ == NonbondedForce::NoCutoff) {
+        krf_ = crf_ = 0.0;  // plain Coulomb, every pair
+    } else {
+        krf_ = (er - 1.0) / ((2.0 * er + 1.0) * cutoff_ * cutoff_ * cutoff_);
+        crf_ = 3.0 * er / ((2.0 * er + 1.0) * cutoff_);
+    }
 
     CUDA_CHECK(cudaSetDevice(dev_));
     CUDA_CHECK(cudaStreamCreateWithFlags(&s_main_, cudaStreamNonBlocking));
@@ -205,6 +213,11 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     CUDA_CHECK(cudaMallocHost(&h_matrix_, sizeof(double) * (size_t)R_ * R_));
     CUDA_CHECK(cudaMallocHost(&h_reps_, sizeof(RepDev) * (size_t)R_));
     CUDA_CHECK(cudaMallocHost(&h_beta_, sizeof(double)));
+    CUDA_CHECK(cudaMallocHost(&h_ctl_, 2 * sizeof(int)));
+    CUDA_CHECK(cudaMalloc(&d_counts_, 2 * sizeof(long long)));
+    CUDA_CHECK(cudaMemset(d_counts_, 0, 2 * sizeof(long long)));
+    h_ctl_[0] = 1;
+    h_ctl_[1] = 0;
     CUDA_CHECK(cudaMallocHost(&h_status_, sizeof(Status)));
     std::memset(h_pos_, 0, sizeof(double) * 3 * (size_t)n_in_);
     int per = 0;
@@ -231,6 +244,8 @@ Engine::~Engine() {
     cudaFreeHost(h_matrix_);
     cudaFreeHost(h_reps_);
     cudaFreeHost(h_beta_);
+    cudaFreeHost(h_ctl_);
+    if (d_counts_) cudaFree(d_counts_);
     cudaFreeHost(h_status_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
@@ -257,10 +272,40 @@ void Engine::set_all_positions(const double* pos) {
 
 void Engine::set_box(int r, const double* box) {
     if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
-    for (int a = 0; a < 3; a++)
-        if (!(box[a] >= 2.0 * cutoff_))
-            throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
+    if (periodic_)
+        for (int a = 0; a < 3; a++)
+            if (!(box[a] >= 2.0 * (cutoff_ + skin_)))
+                throw Error(1,
+                            "The periodic box must be at least twice the cutoff (plus the list skin) in every dimension");
     for (int a = 0; a < 3; a++) specs_[r].box[a] = box[a];
+    force_build_ = true;  // periodic images move with the box
+    infl_dirty_ = true;
+}
+
+void Engine::update_influence(cudaStream_t st) {
+    if (!infl_dirty_) return;
+    infl_dirty_ = false;
+    if (!use_fft_ || method_ != NonbondedForce::PME) return;
+    for (int r = 0; r < R_; r++) {
+        const RepDev& rd = rep_host_[r];
+        launch_influence(A_.influence + rd.cplx_off / 2, A_.moduli, rd.mod_off, rd.K, specs_[r].box, alpha_, st);
+    }
+    CUDA_CHECK(cudaGetLastError());
+}
+
+void Engine::set_list_skin(double skin) {
+    if (!(skin >= 0.0) || skin > 0.5) throw Error(1, "The list skin must lie in [0, 0.5] nm");
+    if (periodic_)
+        for (int r = 0; r < R_; r++)
+            for (int a = 0; a < 3; a++)
+                if (!(specs_[r].box[a] >= 2.0 * (cutoff_ + skin)))
+                    throw Error(1, "The periodic box must be at least twice the cutoff plus the list skin");
+    if (skin == skin_) return;
+    skin_ = skin;
+    A_.rcl2 = list_cutoff2();
+    A_.skin_half2 = (float)(0.25 * skin_ * skin_);
+    force_build_ = true;
+    destroy_graphs();  // the kernels' arguments are part of the graphs
 }
 
 void Engine::set_param(int r, int which, double v) {
@@ -281,6 +326,28 @@ void Engine::set_displacements(int r, const double* displ) {
     std::memcpy(s.displ.data(), displ, sizeof(double) * 3 * (size_t)s.n);
     // the moving set or its displacement changed: rebuild the layout lazily
     layout_ready_ = false;
+}
+
+// Box constants of a replica.  Without periodic boundaries the inverse box is 0,
+// which makes every minimum image and every wrap the identity (d - L rint(0) = d),
+// and the box 1e30 nm, so that no pair is ever taken to need its own image.
+void Engine::set_box_constants(RepDev& rd, const ReplicaSpec& s) const {
+    for (int a = 0; a < 3; a++) {
+        const double L = periodic_ ? s.box[a] : 1.0e30;
+        rd.box[a] = (float)L;
+        rd.ibox[a] = periodic_ ? (float)(1.0 / L) : 0.0f;
+        rd.boxd[a] = L;
+        rd.iboxd[a] = periodic_ ? 1.0 / L : 0.0;
+    }
+}
+
+// Squared cutoffs of the pair kernel and of the list builds (NoCutoff: every pair;
+// 1e29 nm^2 stays below the 3e30 nm^2 at which padding slots are parked).
+float Engine::cutoff2() const {
+    return method_ == NonbondedForce::NoCutoff ? 1.0e29f : (float)(cutoff_ * cutoff_);
+}
+float Engine::list_cutoff2() const {
+    return method_ == NonbondedForce::NoCutoff ? 1.0e29f : (float)((cutoff_ + skin_) * (cutoff_ + skin_));
 }
 
 // ---------------------------------------------------------------------------
@@ -345,12 +412,25 @@ void Engine::build_layout() {
             if (cls[i] == 0) mol[find(i)].push_back(i);
         std::vector<std::pair<uint64_t, int>> keys;
         const int bits = 10;
+        // the cube the curve spans: the periodic box, or the positions' bounding box
+        double lo[3] = {0, 0, 0}, span[3] = {s.box[0], s.box[1], s.box[2]};
+        if (!periodic_) {
+            double hi[3];
+            for (int a = 0; a < 3; a++) lo[a] = hi[a] = s.n ? pos[a] : 0.0;
+            for (int i = 0; i < s.n; i++)
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = std::min(lo[a], pos[3 * i + a]);
+                    hi[a] = std::max(hi[a], pos[3 * i + a]);
+                }
+            for (int a = 0; a < 3; a++) span[a] = std::max(hi[a] - lo[a], 1e-6) * (1.0 + 1e-9);
+        }
         for (auto& kv : mol) {
             int i = kv.second[0];
             uint32_t c[3];
             for (int a = 0; a < 3; a++) {
-                double L = s.box[a];
-                double x = pos[3 * i + a] - L * std::floor(pos[3 * i + a] / L);
+                double L = span[a];
+                double x = pos[3 * i + a] - lo[a];
+                if (periodic_) x -= L * std::floor(x / L);
                 long v = (long)(x / L * (1 << bits));
                 c[a] = (uint32_t)std::min(std::max(v, 0L), (long)(1 << bits) - 1);
             }
@@ -477,13 +557,8 @@ void Engine::build_layout() {
         rd.exc_cta_e = (int)exc_cta_first_.size();
 
         // box and constants
-        for (int a = 0; a < 3; a++) {
-            rd.box[a] = (float)s.box[a];
-            rd.ibox[a] = (float)(1.0 / s.box[a]);
-            rd.boxd[a] = s.box[a];
-            rd.iboxd[a] = 1.0 / s.box[a];
-            rd.K[a] = s.grid[a];
-        }
+        set_box_constants(rd, s);
+        for (int a = 0; a < 3; a++) rd.K[a] = s.grid[a];
         double q2 = 0;
         for (int i = 0; i < s.n; i++) q2 += s.q[i] * s.q[i];
         rd.e_self = (method_ == NonbondedForce::PME) ? -kOne4PiEps0 * alpha_ / std::sqrt(kPi) * q2 : 0.0;
@@ -607,6 +682,10 @@ void Engine::build_layout() {
         if (g.inv) cufftDestroy(g.inv);
     }
     groups_.clear();
+    fft_tw_.clear();
+    fft_plane_.clear();
+    fft_conv_.clear();
+    use_fft_ = false;
     if (method_ == NonbondedForce::PME) {
         std::vector<int> order(R_);
         std::iota(order.begin(), order.end(), 0);
@@ -638,19 +717,49 @@ void Engine::build_layout() {
                 bspline_moduli(rd.K[a], m);
                 rd.mod_off[a] = (int)moduli_.size();
                 for (double v : m) moduli_.push_back((float)v);
+                // FFT twiddles w_N^k = exp(-2 pi i k / N), computed in FP64
+                rd.tw_off[a] = (int)fft_tw_.size();
+                for (int k = 0; k < rd.K[a]; k++) {
+                    const double t = -2.0 * kPi * k / rd.K[a];
+                    fft_tw_.push_back(make_float2((float)std::cos(t), (float)std::sin(t)));
+                }
             }
         }
         build_bricks();
+        // the hand-written transforms need a grid plane (two buffers) in shared memory
+        int smem_max = 0;
+        CUDA_CHECK(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
+        fft_plane_smem_ = fft_conv_smem_ = 0;
+        use_fft_ = true;
+        for (int r = 0; r < R_; r++) {
+            const RepDev& rd = rep_host_[r];
+            const int b = fft_plane_smem_bytes(rd.K[1], rd.K[2]);
+            fft_plane_smem_ = std::max(fft_plane_smem_, b);
+            if (b > smem_max - 1024) use_fft_ = false;
+        }
         for (int r = 0; r < R_; r++) {
             RepDev& rd = rep_host_[r];
             long long C3 = (long long)rd.K[0] * rd.K[1] * (rd.K[2] / 2 + 1);
-            rd.conv_cta_b = (int)conv_cta_rep_.size();
-            const long long per = 4096;
-            for (long long k = 0; k < C3; k += per) {
-                conv_cta_rep_.push_back(r);
-                conv_cta_first_.push_back(k);
+            rd.conv_cta_b = use_fft_ ? (int)fft_conv_.size() : (int)conv_cta_rep_.size();
+            if (use_fft_) {
+                for (int g = 0; g < 2; g++)
+                    for (int x = 0; x < rd.K[0]; x++) fft_plane_.push_back(make_int2(r, g * rd.K[0] + x));
+                // kz chunks of the (x, kz) slab of both grids small enough for two CTAs per SM
+                const int K2h = rd.K[2] / 2 + 1;
+                int nz = K2h;
+                while (nz > 1 && fft_conv_smem_bytes(rd.K[0], nz) > 100 * 1024) nz = (nz + 1) / 2;
+                for (int ky = 0; ky < rd.K[1]; ky++)
+                    for (int z0 = 0; z0 < K2h; z0 += nz) fft_conv_.push_back(make_int4(r, ky, z0, std::min(K2h, z0 + nz)));
+                fft_conv_smem_ = std::max(fft_conv_smem_, fft_conv_smem_bytes(rd.K[0], nz));
+                rd.conv_cta_e = (int)fft_conv_.size();
+            } else {
+                const long long per = 4096;
+                for (long long k = 0; k < C3; k += per) {
+                    conv_cta_rep_.push_back(r);
+                    conv_cta_first_.push_back(k);
+                }
+                rd.conv_cta_e = (int)conv_cta_rep_.size();
             }
-            rd.conv_cta_e = (int)conv_cta_rep_.size();
         }
     } else {
         for (int r = 0; r < R_; r++) {
@@ -660,7 +769,8 @@ void Engine::build_layout() {
     for (int r = 0; r < R_; r++) {
         const ReplicaSpec& s = specs_[r];
         rep_host_[r].e_disp = 0.0;
-        if (s.dispersion) rep_host_[r].e_disp = dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]);
+        if (s.dispersion && periodic_)
+            rep_host_[r].e_disp = dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]);
     }
     if (tile_cap_ == 0) tile_cap_ = nrows_ * 56 + 8192;
     layout_ready_ = true;
@@ -826,7 +936,9 @@ void Engine::alloc_device() {
     a.n_in = n_in_;
     a.full = full_ ? 1 : 0;
     a.method = method_;
-    a.rc2 = (float)(cutoff_ * cutoff_);
+    a.rc2 = cutoff2();
+    a.rcl2 = list_cutoff2();
+    a.skin_half2 = (float)(0.25 * skin_ * skin_);
     a.tile_dynamic = tile_dynamic();
     a.alpha = (float)alpha_;
     a.krf = (float)krf_;
@@ -850,6 +962,14 @@ void Engine::alloc_device() {
     a.displ = dupload(d_allocs_, displ_sorted_);
     a.posq = dalloc<float4>(d_allocs_, NA_);
     a.posq2 = full_ ? dalloc<float4>(d_allocs_, NA_) : nullptr;
+    a.posq_ref = dalloc<float4>(d_allocs_, NA_);
+    a.list_counts = d_counts_;
+    {
+        int* ctl = dalloc<int>(d_allocs_, 2);
+        CUDA_CHECK(cudaMemset(ctl, 0, 2 * sizeof(int)));
+        a.list_ctl = ctl;
+    }
+    force_build_ = true;  // new buffers hold no lists
     a.block_rep = dupload(d_allocs_, block_rep_);
     a.block_cls = dupload(d_allocs_, block_cls_);
     a.block_d = dupload(d_allocs_, block_d_);
@@ -898,7 +1018,16 @@ void Engine::alloc_device() {
         a.qreal = dalloc<float>(d_allocs_, n_real_);
         a.qcplx = dalloc<float2>(d_allocs_, n_cplx_);
         a.moduli = dupload(d_allocs_, moduli_);
-        a.conv_ctas = (int)conv_cta_rep_.size();
+        a.use_fft = use_fft_ ? 1 : 0;
+        a.fft_tw = dupload(d_allocs_, fft_tw_);
+        a.fft_plane_ctas = (int)fft_plane_.size();
+        a.fft_plane = dupload(d_allocs_, fft_plane_);
+        a.fft_plane_smem = fft_plane_smem_;
+        a.fft_conv = dupload(d_allocs_, fft_conv_);
+        a.fft_conv_smem = fft_conv_smem_;
+        a.influence = use_fft_ ? dalloc<float>(d_allocs_, n_cplx_ / 2) : nullptr;
+        infl_dirty_ = true;
+        a.conv_ctas = use_fft_ ? (int)fft_conv_.size() : (int)conv_cta_rep_.size();
         a.conv_cta_rep = dupload(d_allocs_, conv_cta_rep_);
         // per-CTA [first, last) element ranges within each replica's spectrum
         std::vector<long long> pairs(2 * conv_cta_rep_.size());
@@ -913,6 +1042,7 @@ void Engine::alloc_device() {
         a.conv_cta_first = dupload(d_allocs_, pairs);
         a.e_part_conv = dalloc<double>(d_allocs_, 2 * (size_t)std::max(1, a.conv_ctas));
         for (auto& g : groups_) {
+            if (use_fft_) break;  // library plans only for grids beyond the hand-written transforms
             int n[3] = {g.K[0], g.K[1], g.K[2]};
             long long G3 = (long long)n[0] * n[1] * n[2];
             long long C3 = (long long)n[0] * n[1] * (n[2] / 2 + 1);
@@ -934,14 +1064,9 @@ void Engine::update_rep_table() {
     for (int r = 0; r < R_; r++) {
         RepDev& rd = rep_host_[r];
         const ReplicaSpec& s = specs_[r];
-        for (int a = 0; a < 3; a++) {
-            rd.box[a] = (float)s.box[a];
-            rd.ibox[a] = (float)(1.0 / s.box[a]);
-            rd.boxd[a] = s.box[a];
-            rd.iboxd[a] = 1.0 / s.box[a];
-        }
+        set_box_constants(rd, s);
         for (int k = 0; k < NUM_GLOBALS; k++) rd.params[k] = s.params[k];
-        rd.e_disp = s.dispersion ? dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]) : 0.0;
+        rd.e_disp = s.dispersion && periodic_ ? dispersion_coefficient(s) / (s.box[0] * s.box[1] * s.box[2]) : 0.0;
     }
     std::memcpy(h_reps_, rep_host_.data(), sizeof(RepDev) * (size_t)R_);
     *h_beta_ = beta_;
@@ -959,9 +1084,11 @@ int Engine::tile_dynamic() const {
 }
 
 int Engine::launches_per_eval() const {
-    // prepare, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)
-    int n = 4 + 4;
-    if (method_ == NonbondedForce::PME) n += 3;  // spread, conv, gather (moving atoms included)
+    // prepare, decide, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)
+    int n = 4 + 5;  // + the list decision
+    // spread, gather (moving atoms included) and the transforms: three of ours
+    // (zy, x + convolution, inverse yz), or the convolution between library ones
+    if (method_ == NonbondedForce::PME) n += use_fft_ ? 5 : 3;
     return n;
 }
 
@@ -973,7 +1100,9 @@ void Engine::record(cudaStream_t st, bool host_io) {
     }
     CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
     launch_prepare(a, st);
+    launch_decide(a, st);
     bool pme = method_ == NonbondedForce::PME;
     if (pme) {
         // the PME chain on its own stream (overlapping the pair tiles) or in line,
@@ -983,19 +1112,11 @@ void Engine::record(cudaStream_t st, bool host_io) {
             CUDA_CHECK(cudaEventRecord(ev_fork_, st));
             CUDA_CHECK(cudaStreamWaitEvent(s_pme_, ev_fork_, 0));
         }
-        for (auto& g : groups_) {
-            CUFFT_CHECK(cufftSetStream(g.fwd, ps));
-            CUFFT_CHECK(cufftSetStream(g.inv, ps));
-        }
         // the exceptions need neither lists nor grids: they go first on this
         // stream, beside the list building
         launch_exceptions(a, ps);
         launch_spread(a, ps);
-        for (auto& g : groups_)
-            CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
-        launch_conv(a, ps);
-        for (auto& g : groups_)
-            CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
+        pme_transforms(ps);
         launch_gather(a, ps);
         if (tune_pme_stream_) CUDA_CHECK(cudaEventRecord(ev_join_, s_pme_));
     }
@@ -1028,17 +1149,47 @@ void Engine::record(cudaStream_t st, bool host_io) {
     CUDA_CHECK(cudaMemcpyAsync(h_status_, a.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
 }
 
+// Charge grids -> potential grids: the hand-written transforms with the
+// convolution fused in, or (grid planes beyond shared memory) the library's R2C,
+// the convolution kernel and the library's C2R.  mark(name), when given, follows
+// each step (profiling).
+void Engine::pme_transforms(cudaStream_t st, const std::function<void(const char*)>& mark) {
+    const Args& a = A_;
+    if (use_fft_) {
+        launch_fft_forward(a, st);
+        if (mark) mark("fft_zy");
+        launch_fft_conv(a, st);
+        if (mark) mark("fft_x_conv");
+        launch_fft_inverse(a, st);
+        if (mark) mark("ifft_yz");
+        return;
+    }
+    for (auto& g : groups_) {
+        CUFFT_CHECK(cufftSetStream(g.fwd, st));
+        CUFFT_CHECK(cufftSetStream(g.inv, st));
+    }
+    for (auto& g : groups_)
+        CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
+    if (mark) mark("fft_r2c");
+    launch_conv(a, st);
+    if (mark) mark("conv");
+    for (auto& g : groups_)
+        CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
+    if (mark) mark("fft_c2r");
+}
+
 bool Engine::check_status_and_grow() {
     const Status& s = *h_status_;
     last_tiles_ = s.tile_count;
     last_max_row_ = s.max_row;
-    if (!s.overflow) return false;
-    if (s.overflow & 2) {
+    const int overflow = s.overflow | s.sticky;
+    if (!overflow) return false;
+    if (overflow & 2) {
         int want = (int)(s.max_row * 1.25) + 8;
         if (want > 2040) throw Error(6, "A tile row exceeds 2040 tiles: cutoff too large for the block layout");
         row_cap_ = std::max(row_cap_, want);
     }
-    if (s.overflow & 1) tile_cap_ = (int)(std::max(tile_cap_, s.tile_count) * 1.5) + 4096;
+    if (overflow & 1) tile_cap_ = (int)(std::max(tile_cap_, s.tile_count) * 1.5) + 4096;
     alloc_device();
     return true;
 }
@@ -1051,6 +1202,11 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
     }
     for (int attempt = 0; attempt < 4; attempt++) {
         update_rep_table();
+        update_influence(user ? user : s_main_);
+        // the control word is read when the evaluation runs (it follows the
+        // synchronisation that ends every evaluation of this path)
+        h_ctl_[0] = (force_build_ || skin_ <= 0.0) ? 1 : 0;
+        force_build_ = false;
         cudaStream_t st = user ? user : s_main_;
         if (d_pos)
             CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
@@ -1075,8 +1231,10 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
                                            cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
             mark("start");
             launch_prepare(a, st);
+            launch_decide(a, st);
             mark("prepare");
             launch_find(a, st);
             mark("find");
@@ -1085,26 +1243,11 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             launch_exceptions(a, st);
             mark("exceptions");
             if (method_ == NonbondedForce::PME) {
-                for (auto& g : groups_) {
-                    CUFFT_CHECK(cufftSetStream(g.fwd, st));
-                    CUFFT_CHECK(cufftSetStream(g.inv, st));
-                }
                 launch_spread(a, st);
                 mark("spread");
-                for (auto& g : groups_)
-                    CUFFT_CHECK(cufftExecR2C(g.fwd, a.qreal + g.real_off, (cufftComplex*)(a.qcplx + g.cplx_off)));
-                mark("fft_r2c");
-                launch_conv(a, st);
-                mark("conv");
-                for (auto& g : groups_)
-                    CUFFT_CHECK(cufftExecC2R(g.inv, (cufftComplex*)(a.qcplx + g.cplx_off), a.qreal + g.real_off));
-                mark("fft_c2r");
+                pme_transforms(st, mark);
                 launch_gather(a, st);
                 mark("gather");
-                for (auto& g : groups_) {
-                    CUFFT_CHECK(cufftSetStream(g.fwd, s_pme_));
-                    CUFFT_CHECK(cufftSetStream(g.inv, s_pme_));
-                }
             }
             launch_finalize(a, st);
             mark("finalize");
@@ -1149,7 +1292,12 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             CUDA_CHECK(cudaGraphLaunch(gx, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
         }
-        if (!check_status_and_grow()) return;
+        if (!check_status_and_grow()) {
+            // the evaluation has run: later ones (launch_device) leave the build
+            // to the device unless there is no skin
+            h_ctl_[0] = skin_ <= 0.0 ? 1 : 0;
+            return;
+        }
     }
     throw Error(6, "Tile list capacity could not be established");
 }
@@ -1232,6 +1380,39 @@ void Engine::run_device(const double* d_pos, cudaStream_t stream) {
         alloc_device();
     }
     run(false, stream, d_pos);
+}
+
+void Engine::launch_device(const double* d_pos, cudaStream_t stream) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    if (!layout_ready_ || force_build_ || !graph_dev_) {
+        // a new layout, new buffers or a forced build: the synchronous path (it
+        // also establishes the capacities)
+        run_device(d_pos, stream);
+        return;
+    }
+    update_rep_table();
+    update_influence(stream);
+    // the control word stays as the last synchronous evaluation left it: 0 with a
+    // skin (the device decides), 1 without one (every evaluation builds)
+    CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
+                               cudaMemcpyDeviceToDevice, stream));
+    CUDA_CHECK(cudaGraphLaunch(graph_dev_, stream));
+}
+
+bool Engine::poll_overflow() {
+    // the status of the last evaluation (copied to the host at its end); sticky
+    // carries the overflow of every build since the buffers were made
+    if (!check_status_and_grow()) return false;
+    return true;
+}
+
+void Engine::list_counts(long long* evals, long long* builds) const {
+    long long c[2] = {0, 0};
+    CUDA_CHECK(cudaSetDevice(dev_));
+    CUDA_CHECK(cudaDeviceSynchronize());
+    CUDA_CHECK(cudaMemcpy(c, d_counts_, sizeof(c), cudaMemcpyDeviceToHost));
+    if (evals) *evals = c[0];
+    if (builds) *builds = c[1];
 }
 
 void Engine::reorder_from_device(const double* d_pos, cudaStream_t stream) {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -58,6 +59,14 @@ public:
     double param(int r, int which) const { return specs_[r].params[which]; }
     void set_displacements(int r, const double* displ);  // 3n, particle count unchanged
     void set_beta(double beta) { beta_ = beta; }
+    // Neighbour-list skin (nm): lists are built at cutoff + skin and kept until an
+    // atom has moved more than skin / 2 since their build (checked on the device at
+    // every evaluation).  0 (the default): lists are built at every evaluation.
+    void set_list_skin(double skin);
+    void force_build() { force_build_ = true; }
+    double list_skin() const { return skin_; }
+    // evaluations run and how many of them built the lists (synchronises the device)
+    void list_counts(long long* evals, long long* builds) const;
 
     // Host path: positions from the staging copy; outputs to host (nullable).
     void evaluate(double* energies, double* forces, double* forces_nb, double* results, double* matrix);
@@ -70,6 +79,17 @@ public:
     // Device path without output copies: after it returns, forces_device() and
     // results_device() hold the evaluation at d_pos (valid until the next call).
     void run_device(const double* d_pos, cudaStream_t stream);
+    // The same evaluation enqueued on the stream without waiting for it and
+    // without reading its status: the caller synchronises the stream and calls
+    // poll_overflow() before it trusts a result that a list build overflowed
+    // (builds happen at the evaluations where atoms have moved beyond half the
+    // skin, or when forced).
+    void launch_device(const double* d_pos, cudaStream_t stream);
+    // After a synchronisation of the stream of the evaluations: true if a list
+    // build since the last poll overflowed its capacity (the capacities are then
+    // grown and the next evaluation builds the lists again; the results of the
+    // evaluations since that build are wrong and must be redone).
+    bool poll_overflow();
     const double* forces_device() const { return A_.f_out; }
     const double* results_device() const { return A_.results; }
     const double* matrix_device() const { return A_.matrix; }
@@ -107,6 +127,9 @@ public:
 
 private:
     void build_layout();
+    void set_box_constants(RepDev& rd, const ReplicaSpec& s) const;
+    float cutoff2() const;
+    float list_cutoff2() const;
     void build_bricks();
     std::string tuning_key() const;
     void apply_tuning(int tile_per_sm, int brick, bool pme_stream);
@@ -117,6 +140,7 @@ private:
     void fill_args();
     void update_rep_table();
     void record(cudaStream_t main, bool host_io);
+    void pme_transforms(cudaStream_t st, const std::function<void(const char*)>& mark = nullptr);
     void run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned = nullptr);
     bool check_status_and_grow();
     void destroy_graphs();
@@ -133,8 +157,12 @@ private:
     int tile_cap_ = 0;
     int last_tiles_ = 0, last_max_row_ = 0;
     int method_ = 0;
+    bool periodic_ = true;
     double cutoff_ = 1.0, alpha_ = 0.0, krf_ = 0.0, crf_ = 0.0;
     double beta_ = 1.0;
+    double skin_ = 0.0;
+    bool force_build_ = true;  // the next evaluation builds the lists
+    long long* d_counts_ = nullptr;  // device: evaluations, list builds (kept across buffer rebuilds)
     bool layout_ready_ = false;
     bool profiling_ = false;
     int tile_grid_ = 0;
@@ -172,6 +200,14 @@ private:
         long long real_off, cplx_off;
     };
     std::vector<FftGroup> groups_;
+    // hand-written transforms: used when every grid plane fits in shared memory
+    bool use_fft_ = false;
+    std::vector<float2> fft_tw_;
+    std::vector<int2> fft_plane_;
+    std::vector<int4> fft_conv_;
+    int fft_plane_smem_ = 0, fft_conv_smem_ = 0;
+    bool infl_dirty_ = true;  // the influence-function table needs computing (new buffers or boxes)
+    void update_influence(cudaStream_t st);
 
     // pinned host staging
     double* h_pos_ = nullptr;      // 3*n_in
@@ -181,6 +217,7 @@ private:
     double* h_matrix_ = nullptr;   // R*R
     RepDev* h_reps_ = nullptr;     // R
     double* h_beta_ = nullptr;
+    int* h_ctl_ = nullptr;         // list control word, copied to the device by every evaluation
     Status* h_status_ = nullptr;
 
     // device buffers

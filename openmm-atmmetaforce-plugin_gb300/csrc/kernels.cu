@@ -80,6 +80,18 @@ __global__ void k_prepare(Args a) {
     float z = (float)(p[2] - R.boxd[2] * floor(p[2] * R.iboxd[2]));
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
+    if (a.skin_half2 > 0.f) {
+        // displacement since the last list build (minimum image: wrapping is no motion)
+        const float4 r = a.posq_ref[s];
+        const float dx = x - r.x - R.box[0] * rintf((x - r.x) * R.ibox[0]);
+        const float dy = y - r.y - R.box[1] * rintf((y - r.y) * R.ibox[1]);
+        const float dz = z - r.z - R.box[2] * rintf((z - r.z) * R.ibox[2]);
+        float d2 = dx * dx + dy * dy + dz * dz;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(FULL_MASK, d2, o));
+        // non-negative floats order as their bit patterns
+        if (lane == 0) atomicMax(&a.status->disp2, __float_as_uint(d2));
+    }
     for (int k = 0; k < 6; k++) a.F[(size_t)k * a.NA + s] = 0ull;
     if (a.adjoint)
         for (int k = 0; k < 3; k++) a.D[(size_t)k * a.NA + s] = 0ull;
@@ -92,13 +104,7 @@ __global__ void k_prepare(Args a) {
         a.posq2[s] = make_float4(x2, y2, z2, q);
         warp_bbox(x2, y2, z2, R, &a.bb_c2[b], &a.bb_h2[b], lane, nreal);
     }
-    if (b == 0 && lane == 0) {
-        a.status->tile_count = 0;
-        a.status->overflow = 0;
-        a.status->max_row = 0;
-        a.status->next_tile = 0;
-        a.status->next_row = 0;
-    }
+    if (b == 0 && lane == 0) a.status->next_tile = 0;
 }
 
 void launch_prepare(const Args& a, cudaStream_t s) {
@@ -106,6 +112,29 @@ void launch_prepare(const Args& a, cudaStream_t s) {
     int blocks = (a.NB * 32 + threads - 1) / threads;
     k_prepare<<<blocks, threads, 0, s>>>(a);
 }
+
+// Whether this evaluation builds the lists: when forced, with no skin, or when an
+// atom has moved more than skin / 2 since the last build (then no pair within the
+// cutoff now was beyond rc + skin then).  A build resets the finder's counters.
+__global__ void k_decide(Args a) {
+    if (threadIdx.x != 0) return;
+    Status* st = a.status;
+    const float d2 = __uint_as_float(st->disp2);
+    const bool build = a.list_ctl[0] != 0 || !(a.skin_half2 > 0.f) || d2 > a.skin_half2;
+    st->sticky |= st->overflow;
+    if (build) {
+        st->tile_count = 0;
+        st->overflow = 0;
+        st->max_row = 0;
+        st->next_row = 0;
+    }
+    st->rebuild = build ? 1 : 0;
+    st->disp2 = 0u;
+    a.list_counts[0]++;
+    if (build) a.list_counts[1]++;
+}
+
+void launch_decide(const Args& a, cudaStream_t s) { k_decide<<<1, 32, 0, s>>>(a); }
 
 // ---------------------------------------------------------------------------
 // find: one warp per row; bounding-box test of block I against candidates J
@@ -352,9 +381,10 @@ __device__ __forceinline__ void make_stencil(float x, float y, float z, const Re
 // stencil point needs a bounds test; the padding belongs to the neighbouring
 // bricks, which add the same atoms themselves, and only the brick's own points
 // are written, each once.  Grids smaller than a padded brick use the same copy
-// unpadded, with per-point tests.  Grid 0: state 1.  Grid 1: state 2 (two-state
-// mode) or the structure-factor update of the moving atoms, -q at x and +q at
-// x + d (difference mode).
+// unpadded, with per-point tests.  Grid 0: state 1.  Grid 1: the structure-
+// factor update of the moving atoms, -q at x and +q at x + d, in both modes
+// (state 2's grid is Q1 + dQ exactly: the non-moving atoms sit at the same grid
+// points in both states and the integer sums are exact).
 constexpr int kBrickThreads = 256;
 constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kBrickPad = kOrder - 1;      // stencil reach below and above a brick
@@ -499,9 +529,9 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     const int npts = e[0] * e[1] * e[2];
     const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
     float* G = a.qreal + R.real_off + (size_t)g * G3;
-    // the structure-factor update has only the moving blocks (the last blocks of
-    // the replica); a brick none of them reaches is written as zeros
-    const bool upd = g == 1 && !a.full;
+    // grid 1, the structure-factor update, has only the moving blocks (the last
+    // blocks of the replica); a brick none of them reaches is written as zeros
+    const bool upd = g == 1;
     const int jbegin = upd ? R.mov_block_begin : R.block_begin;
     if (upd) {
         bool any = false;
@@ -536,8 +566,6 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
         if (J < R.block_end) {
             if (g == 0) {
                 if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e)) ent0 = J << 2;
-            } else if (a.full) {
-                if (box_meets_brick(a.bb_c2[J], a.bb_h2[J], R, o, e)) ent0 = (J << 2) | 2;
             } else if (a.block_cls[J] != 0) {
                 const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
                 const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
@@ -626,13 +654,10 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(Args a) {
         float2 qa = A[k], qb = B[k];
         float na = qa.x * qa.x + qa.y * qa.y;
         ea += (double)(0.5f * wgt * G * na);
-        if (a.full) {
-            eb += (double)(0.5f * wgt * G * (qb.x * qb.x + qb.y * qb.y));
-        } else {
-            eb += (double)(wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y)));
-        }
+        eb += (double)(wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y)));
         A[k] = make_float2(G * qa.x, G * qa.y);
-        B[k] = make_float2(G * qb.x, G * qb.y);
+        // grid 1 holds dQ: its potential is G dQ (difference mode) or state 2's, G (Q1 + dQ)
+        B[k] = a.full ? make_float2(G * (qa.x + qb.x), G * (qa.y + qb.y)) : make_float2(G * qb.x, G * qb.y);
     }
     red[0][threadIdx.x] = ea;
     red[1][threadIdx.x] = eb;
@@ -947,7 +972,8 @@ __global__ void __launch_bounds__(256) k_finalize(Args a) {
         double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
         double E2;
         if (a.full) {
-            E2 = dir2 + x2 + c2 + R.e_self + R.e_disp;
+            // c2 = E_rec2 - E_rec1, summed directly from the structure-factor update
+            E2 = dir2 + x2 + (c1 + c2) + R.e_self + R.e_disp;
         } else {
             E2 = E1 + (dir2 + xd + c2);
         }

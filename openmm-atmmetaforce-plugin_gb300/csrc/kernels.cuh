@@ -64,7 +64,8 @@ struct RepDev {
     int exc_cta_b, exc_cta_e; // exception-kernel CTAs (energy partials)
     int conv_cta_b, conv_cta_e;
     int var_nb;               // the NonbondedForce is in the ATM variable groups
-    int pad0;
+    int tw_off[3];            // FFT twiddle tables of the three grid dimensions
+    int pad0[2];
     double e_self;            // PME self energy (FP64, host)
     double e_disp;            // dispersion correction (FP64, host)
     double params[9];         // ATM globals
@@ -78,11 +79,13 @@ struct __align__(16) ExcParam {
 
 struct Status {
     int tile_count;   // tiles appended by the finder
-    int overflow;     // bit 0: tile list, bit 1: row capacity
+    int overflow;     // bit 0: tile list, bit 1: row capacity (of the last list build)
     int max_row;      // largest row seen
     int next_tile;    // work counter of the pair-tile kernel (tiles handed out)
     int next_row;     // work counter of the tile finder (rows handed out)
-    int pad[3];
+    int rebuild;      // 1: the lists are built in this evaluation
+    unsigned disp2;   // largest squared displacement since the last build (float bits)
+    int sticky;       // overflow bits of every build since the host last cleared them
 };
 
 // Arguments shared by the kernels of one engine (passed by value).
@@ -93,6 +96,13 @@ struct Args {
     // method
     int method;               // 2 reaction field, 4 PME
     float rc2, alpha, krf, crf;
+    // neighbour lists: built at the list cutoff rc + skin and kept while no atom
+    // has moved more than skin / 2 since the build (skin 0: built every evaluation)
+    float rcl2;               // (rc + skin)^2
+    float skin_half2;         // (skin / 2)^2
+    float4* posq_ref;         // NA: positions at the last build
+    const int* list_ctl;      // device control word: [0] = 1 forces a build
+    long long* list_counts;   // device: evaluations, list builds
     double alphad, cutoffd;
     // replicas
     RepDev* reps;
@@ -158,10 +168,21 @@ struct Args {
     float* qreal;             // real grids (charge, then potential)
     float2* qcplx;            // spectra
     const float* moduli;      // B-spline moduli, per replica per dimension
-    double* e_part_conv;      // 2 per CTA
+    double* e_part_conv;      // 2 per CTA: E_rec1, E_rec2 - E_rec1
     int conv_ctas;
+    // library transforms (grids whose planes exceed shared memory): the
+    // convolution kernel's CTAs
     const int* conv_cta_rep;  // replica of each conv CTA
     const long long* conv_cta_first;  // first complex element of each conv CTA
+    // hand-written transforms (pme_fft.cu)
+    int use_fft;              // 1: k_fft_zy / k_fft_x_conv / k_ifft_yz
+    const float2* fft_tw;     // twiddles w_N^k = exp(-2 pi i k / N), per replica and dimension
+    int fft_plane_ctas;       // (grid, x-plane) CTAs of all replicas
+    const int2* fft_plane;    //   (replica, grid * K0 + x)
+    int fft_plane_smem;       // dynamic shared memory of a plane CTA (bytes)
+    const int4* fft_conv;     // conv CTAs: (replica, ky, kz0, kz1)
+    int fft_conv_smem;
+    float* influence;         // influence function per replica, [ky][x][kz] at cplx_off / 2
     long long n_real_total;
     // results
     double* results;          // R * NUM_RES
@@ -170,12 +191,20 @@ struct Args {
 };
 
 void launch_prepare(const Args& a, cudaStream_t s);
+void launch_decide(const Args& a, cudaStream_t s);
 void launch_find(const Args& a, cudaStream_t s);
 void launch_tiles(const Args& a, int grid, cudaStream_t s);
 void launch_exceptions(const Args& a, cudaStream_t s);
 void launch_spread(const Args& a, cudaStream_t s);
 void launch_conv(const Args& a, cudaStream_t s);
 void launch_gather(const Args& a, cudaStream_t s);
+void launch_fft_forward(const Args& a, cudaStream_t s);
+void launch_fft_conv(const Args& a, cudaStream_t s);
+void launch_fft_inverse(const Args& a, cudaStream_t s);
+int fft_plane_smem_bytes(int K1, int K2);
+void launch_influence(float* G, const float* moduli, const int* mod_off, const int* K, const double* box,
+                      double alpha, cudaStream_t s);
+int fft_conv_smem_bytes(int K0, int nz);
 void launch_finalize(const Args& a, cudaStream_t s);
 void launch_output(const Args& a, cudaStream_t s);
 void launch_matrix(const Args& a, cudaStream_t s);

@@ -3,6 +3,8 @@
 // all of it is a few percent of a step next to the ATM evaluation.
 #include "md.h"
 
+#include <sstream>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -502,6 +504,20 @@ MDDriver::MDDriver(const std::vector<const System*>& systems, int device, bool f
     MD_CHECK(cudaEventCreateWithFlags(&ev_terms_, cudaEventDisableTiming));
     upload_terms(systems);
     update_beta();
+    if (opt_.list_skin >= 0.0) {
+        // no larger than the boxes allow (periodic boxes of at least 2 (cutoff + skin))
+        double skin = std::min(opt_.list_skin, 0.5);
+        for (auto* sys : systems) {
+            const ReplicaSpec sp = spec_from_system(*sys);
+            if (sp.method == NonbondedForce::CutoffPeriodic || sp.method == NonbondedForce::PME)
+                for (int a = 0; a < 3; a++) skin = std::min(skin, 0.5 * sp.box[a] - sp.cutoff);
+        }
+        eng_->set_list_skin(std::max(0.0, skin));
+        tuned_ = true;
+    }
+    if (opt_.check_interval < 1) throw Error(1, "The list check interval must be at least one step");
+    // re-sorts are decided at the checks
+    if (opt_.reorder_interval > 0) opt_.check_interval = std::min(opt_.check_interval, opt_.reorder_interval);
 }
 
 MDDriver::~MDDriver() {
@@ -704,6 +720,8 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
     box_d_ = md_upload(allocs_, box);
     rep_off_d_ = md_upload(allocs_, rep_off);
     ke_d_ = md_alloc<double>(allocs_, R_);
+    x_snap_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
+    v_snap_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
 }
 
 MdDev MDDriver::dev_args() const {
@@ -842,7 +860,10 @@ int MDDriver::get_records(long long* steps, double* results, double* matrices, i
     return n;
 }
 
-void MDDriver::compute_forces() {
+// The group-0 terms and the ATM evaluation at the current positions.  sync: wait
+// for the evaluation and grow the list capacities if a build overflowed (then
+// evaluate again); otherwise the evaluation is only enqueued.
+void MDDriver::compute_forces(bool sync) {
     if (!have_positions_) throw Error(3, "Positions have not been set");
     MD_CHECK(cudaSetDevice(dev_));
     // the group-0 terms on their own stream, beside the ATM evaluation (after the
@@ -858,9 +879,37 @@ void MDDriver::compute_forces() {
         MD_CHECK(cudaGetLastError());
     }
     MD_CHECK(cudaEventRecord(ev_terms_, s_terms_));
-    eng_->run_device(x_, s_);  // ends with a synchronisation of s_
+    if (sync) eng_->run_device(x_, s_);  // synchronises and grows capacities as needed
+    else eng_->launch_device(x_, s_);
     MD_CHECK(cudaStreamWaitEvent(s_, ev_terms_, 0));
     forces_valid_ = true;
+}
+
+void MDDriver::snapshot() {
+    MD_CHECK(cudaMemcpyAsync(x_snap_, x_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaMemcpyAsync(v_snap_, v_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToDevice, s_));
+    step_snap_ = step_;
+    rec_count_snap_ = rec_count_;
+    rec_last_snap_ = rec_last_step_;
+}
+
+void MDDriver::restore() {
+    MD_CHECK(cudaMemcpyAsync(x_, x_snap_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaMemcpyAsync(v_, v_snap_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToDevice, s_));
+    step_ = step_snap_;
+    rec_count_ = rec_count_snap_;
+    rec_last_step_ = rec_last_snap_;
+    forces_valid_ = false;
+}
+
+bool MDDriver::check_lists() {
+    MD_CHECK(cudaStreamSynchronize(s_));
+    if (eng_->poll_overflow()) return true;
+    if (opt_.fail_check > 0 && ++checks_ == opt_.fail_check) {
+        // the test hook: handled as an overflow (the lists are built again)
+        eng_->force_build();
+        return true;
+    }
     // re-sort when the pair-tile count shows the atom order has decayed
     int tiles = 0;
     eng_->stats(&tiles, nullptr, nullptr);
@@ -868,19 +917,26 @@ void MDDriver::compute_forces() {
     bool due = opt_.reorder_interval > 0 ? step_ - last_reorder_step_ >= opt_.reorder_interval
                                          : tiles > base_tiles_ + base_tiles_ / 5;
     if (due && step_ > last_reorder_step_) {
-        // the layout is rebuilt at the next evaluation; the forces just computed stay valid
+        // the layout is rebuilt at the next evaluation
         eng_->reorder_from_device(x_, s_);
         reorders_++;
         base_tiles_ = 0;
         last_reorder_step_ = step_;
+        forces_valid_ = false;
     }
+    return false;
 }
 
 void MDDriver::step(int nsteps) {
     if (nsteps < 0) throw Error(1, "Negative step count");
     MD_CHECK(cudaSetDevice(dev_));
-    for (int k = 0; k < nsteps; k++) {
-        if (!forces_valid_) compute_forces();
+    if (nsteps == 0) return;
+    if (!tuned_) autotune(20);
+    if (!forces_valid_) compute_forces(true);
+    snapshot();
+    int since = 0;
+    for (int k = 0; k < nsteps;) {
+        if (!forces_valid_) compute_forces(false);
         record_step();
         MdDev a = dev_args();
         int nb = (n_ + 255) / 256;
@@ -890,7 +946,23 @@ void MDDriver::step(int nsteps) {
         k_md_finish<<<nb, 256, 0, s_>>>(a, x_);
         MD_CHECK(cudaGetLastError());
         step_++;
+        k++;
+        since++;
         forces_valid_ = false;
+        if (since >= opt_.check_interval || k == nsteps) {
+            // the forces of the next step first: their list build is checked too
+            compute_forces(false);
+            if (check_lists()) {
+                // an overflowed build: back to the snapshot, with grown capacities
+                const long long redo = step_ - step_snap_;
+                redos_++;
+                restore();
+                k -= (int)redo;
+                compute_forces(true);
+            }
+            snapshot();
+            since = 0;
+        }
     }
     int failed = 0;
     MD_CHECK(cudaMemcpyAsync(&failed, status_, sizeof(int), cudaMemcpyDeviceToHost, s_));
@@ -902,10 +974,74 @@ void MDDriver::step(int nsteps) {
     }
 }
 
+std::string MDDriver::autotune(int trials) {
+    if (trials < 1) throw Error(1, "trials must be positive");
+    if (!have_positions_) throw Error(3, "Positions have not been set");
+    MD_CHECK(cudaSetDevice(dev_));
+    tuned_ = true;  // the steps below do not tune again
+    std::ostringstream rep;
+    if (!forces_valid_) compute_forces(true);
+    rep << eng_->autotune(3, true);
+    // the state every trial starts from, and that the simulation continues from
+    double *xt = nullptr, *vt = nullptr;
+    const size_t bytes = sizeof(double) * 3 * (size_t)n_;
+    MD_CHECK(cudaMalloc(&xt, bytes));
+    MD_CHECK(cudaMalloc(&vt, bytes));
+    MD_CHECK(cudaMemcpyAsync(xt, x_, bytes, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaMemcpyAsync(vt, v_, bytes, cudaMemcpyDeviceToDevice, s_));
+    const long long s0 = step_, r0 = rec_count_, l0 = rec_last_step_;
+    const int rec = rec_interval_;
+    rec_interval_ = 0;
+    double best_ms = 1e30, best = eng_->list_skin();
+    const double cands[] = {0.0, 0.05, 0.1, 0.15, 0.2};
+    cudaEvent_t e0, e1;
+    MD_CHECK(cudaEventCreate(&e0));
+    MD_CHECK(cudaEventCreate(&e1));
+    for (double skin : cands) {
+        try {
+            eng_->set_list_skin(skin);
+        } catch (const Error&) {
+            continue;  // the box is too small for this skin
+        }
+        MD_CHECK(cudaMemcpyAsync(x_, xt, bytes, cudaMemcpyDeviceToDevice, s_));
+        MD_CHECK(cudaMemcpyAsync(v_, vt, bytes, cudaMemcpyDeviceToDevice, s_));
+        step_ = s0;
+        forces_valid_ = false;
+        step(std::max(2, trials / 4));  // graph capture and capacities
+        MD_CHECK(cudaEventRecord(e0, s_));
+        step(trials);
+        MD_CHECK(cudaEventRecord(e1, s_));
+        MD_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MD_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= trials;
+        rep << "list skin " << skin << " nm: " << ms << " ms/step\n";
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = skin;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    eng_->set_list_skin(best);
+    MD_CHECK(cudaMemcpyAsync(x_, xt, bytes, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaMemcpyAsync(v_, vt, bytes, cudaMemcpyDeviceToDevice, s_));
+    MD_CHECK(cudaStreamSynchronize(s_));
+    cudaFree(xt);
+    cudaFree(vt);
+    step_ = s0;
+    rec_count_ = r0;
+    rec_last_step_ = l0;
+    rec_interval_ = rec;
+    forces_valid_ = false;
+    rep << "chosen: list skin " << best << " nm (" << best_ms << " ms/step)\n";
+    return rep.str();
+}
+
 void MDDriver::get_state(double* pos, double* vel, double* forces, double* potential, double* kinetic,
                          double* results) {
     MD_CHECK(cudaSetDevice(dev_));
-    if ((forces || potential || kinetic || results) && !forces_valid_) compute_forces();
+    if ((forces || potential || kinetic || results) && !forces_valid_) compute_forces(true);
     MD_CHECK(cudaStreamSynchronize(s_terms_));  // the group-0 forces and energies below
     if (pos) MD_CHECK(cudaMemcpy(pos, x_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToHost));
     if (vel) MD_CHECK(cudaMemcpy(vel, v_, sizeof(double) * 3 * (size_t)n_, cudaMemcpyDeviceToHost));

@@ -15,6 +15,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "engine.h"
@@ -69,6 +70,10 @@ struct MdOptions {
     uint64_t seed = 0;
     double constraint_tol = 1e-10;  // relative, on d^2
     int reorder_interval = 0;       // steps between re-sorts (0: when the tile count has grown by 20 %)
+    double list_skin = 0.1;         // pair-list skin (nm, reduced to what the boxes allow); < 0: chosen
+                                    // by autotune() at the first step
+    int check_interval = 20;        // steps between host checks of the list capacities
+    int fail_check = 0;             // test hook: the n-th list check reports an overflow (0: never)
 };
 
 class MDDriver {
@@ -88,12 +93,24 @@ public:
     void set_velocities_to_temperature(double T, uint64_t seed);
     void set_param(int r, int which, double v);
     void set_integrator(double T, double friction, double dt);
+    // Steps are enqueued without a host synchronisation per step: every
+    // check_interval steps (and at the end of the call) the host reads the list
+    // status; if a list build overflowed its capacity, the capacities grow, the
+    // state goes back to the snapshot taken at the previous check and those steps
+    // run again (the thermostat noise is a function of the step, so the redone
+    // steps are the steps that should have run).
     void step(int nsteps);
+    // Times the evaluation's launch space (Engine::autotune) and then `trials`
+    // steps at each candidate pair-list skin (0 to 0.2 nm), keeps the fastest and
+    // returns the report.  The state (positions, velocities, step count,
+    // recording) is restored afterwards.  Needs positions and velocities.
+    std::string autotune(int trials);
     // host outputs, nullable: positions, velocities, total forces (3n each);
     // per replica potential (group 0 + ATM) and kinetic energies; R x NUM_RES
     // results of the ATM evaluation at the current positions
     void get_state(double* pos, double* vel, double* forces, double* potential, double* kinetic, double* results);
     int reorders() const { return reorders_; }
+    int redos() const { return redos_; }  // checks that sent the state back to a snapshot
     // Records of the ATM results (R x NUM_RES) and the R x R reduced-energy matrix
     // (beta = 1/kT of the integrator) every `interval` steps, at the positions the
     // step starts from, kept on the device in a ring of `capacity` records
@@ -107,7 +124,10 @@ public:
     const std::vector<int>& degrees_of_freedom() const { return dof_; }
 
 private:
-    void compute_forces();
+    void compute_forces(bool sync);
+    void snapshot();
+    void restore();
+    bool check_lists();  // synchronises; true if steps since the snapshot must be redone
     void upload_terms(const std::vector<const System*>& systems);
     MdDev dev_args() const;
 
@@ -143,6 +163,10 @@ private:
     double* box_d_ = nullptr;  // 3 per replica
     int* rep_off_d_ = nullptr; // R + 1
     double* ke_d_ = nullptr;   // R
+    double *x_snap_ = nullptr, *v_snap_ = nullptr;  // state at the last list check
+    long long step_snap_ = 0, rec_count_snap_ = 0, rec_last_snap_ = -1;
+    int checks_ = 0, redos_ = 0;
+    bool tuned_ = false;
     int n_bonds_ = 0, n_angles_ = 0, n_posres_ = 0, n_cent_ = 0, n_cons_ = 0, n_settle_ = 0;
     std::vector<int> term_rep_;  // replica of each term, in e_terms_ order
     // recording

@@ -138,7 +138,7 @@ constexpr unsigned kHalfA = 1u << 30, kHalfB = 1u << 31, kSlotBits = kHalfA - 1u
 
 __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, int kind, float4 ci, int lane,
                                               int* list, int from, int natom, const float4* s_ipos) {
-    const float rcm = sqrtf(a.rc2) + kHalfCutMargin;
+    const float rcm = sqrtf(a.rcl2) + kHalfCutMargin;
     const __half2 thr = __float2half2_rn(rcm * rcm);
     const uint4* ih = reinterpret_cast<const uint4*>(s_ipos);
     int kept = from;
@@ -195,7 +195,7 @@ __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, in
 __device__ __noinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
                                          int from, int natom, const float4* s_ipos, bool hcut) {
     if (hcut) return exact_cut_half(a, R, kind, ci, lane, list, from, natom, s_ipos);
-    const float rc2 = a.rc2 * 1.00001f;
+    const float rc2 = a.rcl2 * 1.00001f;
     int kept = from;
     for (int g = from; g < natom; g += 32) {
         const int k = g + lane;
@@ -289,7 +289,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
                     cj4.z += dd.z;
                 }
             }
-            ok = boxes_close(ci, hi, cj4, hj4, R, a.rc2);
+            ok = boxes_close(ci, hi, cj4, hj4, R, a.rcl2);
             if (nex > 32)
                 for (int k = e0; ok && k < e1; k++)
                     if (ee[k].x == Jl) ok = false;
@@ -327,7 +327,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             }
 #pragma unroll
             for (int t = 0; t < 4; t++) {
-                const bool in = lane < n[t] && point_close(ci, hi, p[t], R, a.rc2);
+                const bool in = lane < n[t] && point_close(ci, hi, p[t], R, a.rcl2);
                 const unsigned b = __ballot_sync(FULL_MASK, in);
                 const int k = natom + __popc(b & ((1u << lane) - 1u));
                 if (in && k < cap && !over) out[k] = J[t] * kTile + lane;
@@ -365,8 +365,9 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     float4 ci, hi;
     row_box(a, I, kind, ci, hi);
     // pbc: some pair of an atom tile may need its own minimum image when the
-    // cutoff sphere around block I reaches half a box length
-    const float rc = sqrtf(a.rc2);
+    // cutoff sphere around block I reaches half a box length (at the list cutoff:
+    // while the lists are kept, a block's box grows by up to skin / 2 per side)
+    const float rc = sqrtf(a.rcl2);
     const unsigned pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
                           rc + 2.f * hi.z >= 0.5f * R.box[2])
                              ? 1u
@@ -477,6 +478,10 @@ __global__ void __launch_bounds__(kFindWarps * 32, 6) k_find(Args a) {
     __shared__ int s_stage[kFindWarps][kStageAtoms];
     __shared__ float4 s_ipos[kFindWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (!a.status->rebuild) return;  // the lists of an earlier evaluation still hold
+    if (a.skin_half2 > 0.f)  // the positions of this build, for the displacement test
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.NA; s += gridDim.x * blockDim.x)
+            a.posq_ref[s] = a.posq[s];
     // the first row of every warp is fixed, the later ones come from the counter
     const int nw = (gridDim.x * blockDim.x) >> 5;
     int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -613,6 +618,162 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
     }
 }
 
+// Two FP32 values in one 64-bit register pair, for the packed FP32 instructions
+// of the sm_100 family (add / mul / fma .rn.f32x2: one instruction, two lanes of
+// arithmetic, each rounded exactly as its scalar form).  lo = first, hi = second.
+typedef unsigned long long f2x;
+
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float f2_lo(f2x v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return lo;
+}
+__device__ __forceinline__ float f2_hi(f2x v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return hi;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+    f2x d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
+    f2x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+    f2x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_splat(float v) { return f2_pack(v, v); }
+
+// Entries of the packed j layout of one half tile: entry m (0..15) holds j-slots
+// m & 7 and (m & 7) + 8 side by side, as three 16-byte words
+// {x, x', y, y'}, {z, z', q, q'}, {s, s', e, e'} (s = sigma/2, e = 2 sqrt(eps)).
+constexpr int kPackedWords = 3;
+
+// Lane l of a half (its j-slot data pj, lj) writes its slot into the two entries
+// that carry it (entries l & 7 and (l & 7) + 8, component l >= 8).
+__device__ __forceinline__ void store_packed_j(float4* se, int l, float4 pj, float2 lj) {
+    const int c = l >> 3;
+    float* e0 = reinterpret_cast<float*>(se + kPackedWords * (l & 7));
+    float* e1 = reinterpret_cast<float*>(se + kPackedWords * ((l & 7) + 8));
+    const float v[6] = {pj.x, pj.y, pj.z, pj.w, lj.x, lj.y};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        e0[2 * q + c] = v[q];
+        e1[2 * q + c] = v[q];
+    }
+}
+
+// The hot tile variant (atom tiles of state rows, no per-pair images, no mask:
+// padding j slots parked far away) with two pairs per instruction: lane l of a
+// half meets j-slots e = (l + k) & 7 and e + 8 at step k (8 steps, entry
+// (l & 7) + k of the packed layout: a constant offset per unrolled step).  Within
+// each group of 8 lanes of a half the j-force sums travel with their entry by
+// shuffles; after the 8 steps lane l holds entry l & 7, and the two groups' sums
+// of that entry are added, so that lane l returns the j force of its own slot l.
+//   MASKED: smask holds, per j-slot s (bit s), whether the pair (this lane's i,
+//   slot s) is counted (exclusion sub-tiles; excluded pairs, self pairs included,
+//   are evaluated at r^2 = 1e30 like pairs beyond the cutoff).
+template <int METHOD, bool MASKED>
+__device__ __forceinline__ void tile_steps_x2(const float4* __restrict__ se, float4 pi, float2 li, int lane,
+                                              unsigned smask, float rc2, float alpha, float krf, float crf,
+                                              float3& fi, float3& fj, float& e32) {
+    const int src = (lane & ~7) | ((lane + 1) & 7);  // next lane of this group of 8
+    const f2x px = f2_splat(pi.x), py = f2_splat(pi.y), pz = f2_splat(pi.z), pq = f2_splat(pi.w);
+    const f2x ps = f2_splat(li.x), pe = f2_splat(li.y);
+    f2x fix = 0ull, fiy = 0ull, fiz = 0ull, fjx = 0ull, fjy = 0ull, fjz = 0ull, eacc = 0ull;
+    const float4* base = se + kPackedWords * (lane & 7);
+#pragma unroll 4
+    for (int k = 0; k < 8; k++) {
+        const ulonglong2 w0 = *reinterpret_cast<const ulonglong2*>(base + kPackedWords * k);
+        const ulonglong2 w1 = *reinterpret_cast<const ulonglong2*>(base + kPackedWords * k + 1);
+        const ulonglong2 w2 = *reinterpret_cast<const ulonglong2*>(base + kPackedWords * k + 2);
+        const f2x dx = f2_sub(w0.x, px), dy = f2_sub(w0.y, py), dz = f2_sub(w1.x, pz);
+        const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+        const float ra = f2_lo(r2), rb = f2_hi(r2);
+        bool ia = ra < rc2, ib = rb < rc2;
+        if (MASKED) {
+            const int sa = ((lane & 7) + k) & 7;  // slots sa and sa + 8 of this step
+            ia = ia && ((smask >> sa) & 1u);
+            ib = ib && ((smask >> (sa + 8)) & 1u);
+        }
+        const f2x qq = f2_mul(pq, w1.y), sig = f2_add(ps, w2.x), eps4 = f2_mul(pe, w2.y);
+        f2x e, fr;
+        if (METHOD == 4) {
+            // a pair not counted is evaluated at r^2 = 1e30 nm^2, where every term is exactly zero
+            const f2x r2s = f2_pack(ia ? ra : 1.0e30f, ib ? rb : 1.0e30f);
+            const f2x invr = f2_pack(rsqrt_ftz(f2_lo(r2s)), rsqrt_ftz(f2_hi(r2s)));
+            const f2x invr2 = f2_mul(invr, invr);
+            const f2x s2 = f2_mul(f2_mul(sig, sig), invr2);
+            const f2x s6 = f2_mul(f2_mul(s2, s2), s2);
+            const f2x t6 = f2_mul(eps4, s6);
+            const f2x xa = f2_mul(r2s, f2_splat(-alpha * alpha * kLog2e));
+            const f2x ex = f2_pack(ex2_ftz(f2_lo(xa)), ex2_ftz(f2_hi(xa)));
+            const f2x den = f2_fma(f2_splat(0.3275911f * alpha), f2_mul(r2s, invr), f2_splat(1.0f));
+            const f2x t = f2_pack(rcp_ftz(f2_lo(den)), rcp_ftz(f2_hi(den)));
+            f2x p = f2_fma(t, f2_splat(1.061405429f), f2_splat(-1.453152027f));
+            p = f2_fma(t, p, f2_splat(1.421413741f));
+            p = f2_fma(t, p, f2_splat(-0.284496736f));
+            p = f2_fma(t, p, f2_splat(0.254829592f));
+            const f2x ec = f2_mul(f2_mul(f2_mul(t, p), ex), invr);
+            e = f2_fma(qq, ec, f2_fma(t6, s6, f2_sub(0ull, t6)));
+            const f2x lj = f2_fma(s6, f2_splat(12.0f), f2_splat(-6.0f));
+            const f2x cq = f2_mul(qq, f2_fma(f2_splat(1.1283791670955126f * alpha), ex, ec));
+            fr = f2_mul(f2_fma(t6, lj, cq), invr2);
+        } else {
+            // reaction field: terms at r^2 (or 1 when not counted), then zeroed by the weight
+            const f2x r2s = f2_pack(ia ? ra : 1.0f, ib ? rb : 1.0f);
+            const f2x w = f2_pack(ia ? 1.0f : 0.0f, ib ? 1.0f : 0.0f);
+            const f2x invr = f2_pack(rsqrt_ftz(f2_lo(r2s)), rsqrt_ftz(f2_hi(r2s)));
+            const f2x invr2 = f2_mul(invr, invr);
+            const f2x s2 = f2_mul(f2_mul(sig, sig), invr2);
+            const f2x s6 = f2_mul(f2_mul(s2, s2), s2);
+            const f2x t6 = f2_mul(eps4, s6);
+            const f2x elj = f2_fma(t6, s6, f2_sub(0ull, t6));
+            const f2x ec = f2_add(f2_fma(f2_splat(krf), r2s, invr), f2_splat(-crf));
+            e = f2_mul(f2_fma(qq, ec, elj), w);
+            // -(dE/dr)/r: LJ (12 t6 s6 - 6 t6) / r^2, Coulomb qq (1/r^3 - 2 krf)
+            const f2x flj = f2_mul(t6, f2_fma(s6, f2_splat(12.0f), f2_splat(-6.0f)));
+            const f2x fc = f2_mul(qq, f2_fma(invr, invr2, f2_splat(-2.0f * krf)));
+            fr = f2_mul(f2_fma(flj, invr2, fc), w);
+        }
+        eacc = f2_add(eacc, e);
+        fix = f2_fma(fr, dx, fix);
+        fiy = f2_fma(fr, dy, fiy);
+        fiz = f2_fma(fr, dz, fiz);
+        fjx = __shfl_sync(FULL_MASK, f2_fma(fr, dx, fjx), src);
+        fjy = __shfl_sync(FULL_MASK, f2_fma(fr, dy, fjy), src);
+        fjz = __shfl_sync(FULL_MASK, f2_fma(fr, dz, fjz), src);
+    }
+    // the other group of this half holds the same entry: add its sums, keep this lane's slot
+    fjx = f2_add(fjx, __shfl_xor_sync(FULL_MASK, fjx, 8));
+    fjy = f2_add(fjy, __shfl_xor_sync(FULL_MASK, fjy, 8));
+    fjz = f2_add(fjz, __shfl_xor_sync(FULL_MASK, fjz, 8));
+    const bool upper = lane & 8;
+    fj.x = upper ? f2_hi(fjx) : f2_lo(fjx);
+    fj.y = upper ? f2_hi(fjy) : f2_lo(fjy);
+    fj.z = upper ? f2_hi(fjz) : f2_lo(fjz);
+    fi.x = -(f2_lo(fix) + f2_hi(fix));
+    fi.y = -(f2_lo(fiy) + f2_hi(fiy));
+    fi.z = -(f2_lo(fiz) + f2_hi(fiz));
+    e32 = f2_lo(eacc) + f2_hi(eacc);
+}
+
 // Difference tiles with the adjoint: besides energy and forces, the derivatives
 // of the pair energy with respect to each partner's scaled charge, sigma and
 // epsilon (LJ: dphi/dsigma_i = eps4 (6 s^12 - 3 s^6) / sigma_ij,
@@ -677,8 +838,10 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
 
 template <int METHOD, bool DYN>
 __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
-    __shared__ float4 s_p[kTileThreads / 32][64];
-    __shared__ float2 s_l[kTileThreads / 32][64];
+    // per warp: the j data of its two half tiles, either doubled (64 float4
+    // positions + 64 float2 LJ pairs) or in the packed layout (2 x 16 entries of 3
+    // float4), 1536 bytes either way
+    __shared__ float4 s_buf[kTileThreads / 32][96];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int hf = lane >> 4, l = lane & (kHalf - 1);  // half of the warp, lane within it
     int ntiles = a.status->tile_count;
@@ -764,19 +927,34 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         if (!masked_h && !jvalid) pj.x = pj.y = pj.z = 1.0e15f;
         const bool masked = __any_sync(FULL_MASK, masked_h);
         const bool pbc_w = __any_sync(FULL_MASK, pbc);
-        s_p[w][32 * hf + l] = pj;
-        s_p[w][32 * hf + l + kHalf] = pj;
-        s_l[w][32 * hf + l] = lj;
-        s_l[w][32 * hf + l + kHalf] = lj;
+        // state rows without per-pair images (both halves) run two pairs per
+        // instruction on the packed layout, masked or not
+        const bool packed = !diff && !pbc_w;
+        float4* s_p = s_buf[w];
+        float2* s_l = reinterpret_cast<float2*>(s_buf[w] + 64);
+        if (packed) {
+            store_packed_j(s_buf[w] + 48 * hf, l, pj, lj);
+        } else {
+            s_p[32 * hf + l] = pj;
+            s_p[32 * hf + l + kHalf] = pj;
+            s_l[32 * hf + l] = lj;
+            s_l[32 * hf + l + kHalf] = lj;
+        }
         __syncwarp();
-        const float4* spl = &s_p[w][32 * hf + l];
-        const float2* sll = &s_l[w][32 * hf + l];
+        const float4* spl = s_p + 32 * hf + l;
+        const float2* sll = s_l + 32 * hf + l;
         float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
         float3 ai = make_float3(0.f, 0.f, 0.f), aj = make_float3(0.f, 0.f, 0.f);
         float e32 = 0.f;
         double e64 = 0.0;
         const bool adj = diff && a.adjoint;
-        if (adj) {
+        if (packed && masked) {
+            // the lane's mask (bit k: slot (l + k) & 15) rotated to slot order (bit s: slot s)
+            const unsigned sm = ((mask << l) | (mask >> (kHalf - l))) & 0xffffu;
+            tile_steps_x2<METHOD, true>(s_buf[w] + 48 * hf, pi, li, lane, sm, rc2, alpha, krf, crf, fi, fj, e32);
+        } else if (packed) {
+            tile_steps_x2<METHOD, false>(s_buf[w] + 48 * hf, pi, li, lane, 0u, rc2, alpha, krf, crf, fi, fj, e32);
+        } else if (adj) {
             if (pbc_w)
                 tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
                                              crf, fi, fj, e64, ai, aj);
@@ -806,16 +984,25 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         }
         __syncwarp();
         const bool diag = !atom_tile && T.y == I16;
-        // tile energy over the half, in FP64 and a fixed order: the difference tiles
-        // sum every pair term in FP64 (their sum is u); the state tiles keep one FP32
-        // partial of 16 pair terms per lane (FP64 arithmetic is scarce on this part)
-        // and sum the partials in FP64, so that u = E2 - E1 of the two-state mode is a
-        // difference of FP64 sums
-        double esum = diff ? e64 : (double)(diag ? 0.5f * e32 : e32);
+        // tile energy over the half, in a fixed order: FP64 on the difference tiles
+        // (their sum is u); FP32 on the state tiles (FP64 arithmetic is scarce on
+        // this part).  In the two-state mode the state-1 and state-2 tiles of atoms
+        // that do not move are the same tiles with the same bits (their j lists
+        // differ only in the moving atoms, which come last), so their FP32 sums
+        // cancel exactly in u = E2 - E1, which the FP64 row and replica sums carry.
+        double esum;
+        if (diff) {
+            esum = e64;
 #pragma unroll
-        for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+            for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+        } else {
+            float es = diag ? 0.5f * e32 : e32;
+#pragma unroll
+            for (int o = kHalf / 2; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
+            esum = (double)es;
+        }
         const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
-        if (l == 0) a.e_tile[(size_t)row * a.row_cap + slot] = sign * esum;
+        if (l == 0) a.e_tile[(size_t)row * a.row_cap + slot] = kind == ROW_DIFF1 ? -esum : esum;
         if (!atom_tile || aux > 0) {  // (an empty tile, the filler of an odd row, adds nothing)
         unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
         fix_add_t(Fp + i, sign * fi.x);

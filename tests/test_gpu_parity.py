@@ -77,6 +77,17 @@ def test_reaction_field_2394(diff):
 
 
 @pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+@pytest.mark.parametrize("method", [S.NOCUTOFF, S.CUTOFF_NONPERIODIC], ids=["no-cutoff", "cutoff-nonperiodic"])
+def test_nonperiodic_methods(method, diff):
+    """NoCutoff (plain Coulomb + LJ over every pair) and CutoffNonPeriodic
+    (reaction field within the cutoff), no periodic images: the inner
+    NonbondedForce the reference re-evaluates may use either."""
+    c = S.water_ligand_box(2394, 3.0, [24], [(1.5, 1.5, 1.5)], method, 0.9, seed=5,
+                           params=S.default_params(0.4, 0.6, 0.05, 10.0, 0.0))
+    check_case(c, diff)
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
 def test_pme_small(diff):
     c = S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=11,
                            params=S.default_params(0.2, 0.7, 0.1, 30.0, 2.0))
