@@ -27,7 +27,8 @@ def system_from_case(case, nonbonded_group=1, atm_group=2, mass=1.0):
     for m in masses:
         sys_.addParticle(m)
     L = spec.box
-    sys_.setDefaultPeriodicBoxVectors((L[0], 0, 0), (0, L[1], 0), (0, 0, L[2]))
+    t = getattr(spec, "tilt", (0.0, 0.0, 0.0))  # reduced triclinic box vectors
+    sys_.setDefaultPeriodicBoxVectors((L[0], 0, 0), (t[0], L[1], 0), (t[1], t[2], L[2]))
     nb = NonbondedForce()
     for i in range(case.n):
         nb.addParticle(spec.charge[i], spec.sigma[i], spec.epsilon[i])

@@ -70,6 +70,9 @@ class NonbondedSpec:
     cutoff: float
     box: np.ndarray
     eps_rf: float = 78.5
+    # b_x, c_x, c_y of OpenMM's reduced triclinic box vectors a = (box0, 0, 0),
+    # b = (b_x, box1, 0), c = (c_x, c_y, box2); zeros for an orthorhombic box
+    tilt: tuple = (0.0, 0.0, 0.0)
     ewald_tol: float = 5e-4
     alpha: float = 0.0
     grid: tuple = (0, 0, 0)
@@ -158,6 +161,27 @@ def _ligand_params(rng, n):
 
 def _min_image(d, box):
     return d - box * np.round(d / box)
+
+
+def box_vectors(box, tilt=(0.0, 0.0, 0.0)):
+    """The 3 x 3 box vectors (rows a, b, c) of a box diagonal and its tilts."""
+    return np.array([[box[0], 0.0, 0.0], [tilt[0], box[1], 0.0], [tilt[1], tilt[2], box[2]]], dtype=np.float64)
+
+
+def min_image_triclinic(d, box, tilt):
+    """OpenMM's minimum image in a reduced triclinic box: subtract c, then b,
+    then a, each rounded to the nearest multiple (d: (..., 3))."""
+    d = np.array(d, dtype=np.float64, copy=True)
+    k = np.floor(d[..., 2] / box[2] + 0.5)
+    d[..., 0] -= k * tilt[1]
+    d[..., 1] -= k * tilt[2]
+    d[..., 2] -= k * box[2]
+    k = np.floor(d[..., 1] / box[1] + 0.5)
+    d[..., 0] -= k * tilt[0]
+    d[..., 1] -= k * box[1]
+    k = np.floor(d[..., 0] / box[0] + 0.5)
+    d[..., 0] -= k * box[0]
+    return d
 
 
 def water_ligand_box(n_total, box_edge, ligand_sizes, displacements, method, cutoff, seed,
@@ -427,3 +451,94 @@ def md_terms_ligand_centroid(case, kf=25.0, tol=0.15, bond_k=2.5e5, angle_k=500.
             cent.append((np.array([int(i)]), g2, float(kf), float(tol), np.zeros(3)))
     terms.centroid = cent
     return terms, pos
+
+
+
+def triclinic_water_ligand_box(n_total, box, tilt, ligand_sizes, displacements, method, cutoff, seed, params=None,
+                               eps_rf=78.5, ewald_tol=5e-4, name=""):
+    """A triclinic box (OpenMM's reduced form: box diagonal ``box``, tilts b_x,
+    c_x, c_y) of ``n_total`` atoms with the distributions of
+    ``water_ligand_box``: water oxygens on a jittered lattice of fractional
+    coordinates mapped through the box vectors (rigid water geometry kept),
+    cavities of 0.3 nm (triclinic minimum image) around every ligand atom at both
+    end states.  The PME grid follows OpenMM's rule on the box diagonal."""
+    rng = np.random.default_rng(seed)
+    box = np.asarray(box, dtype=np.float64)
+    tilt = np.asarray(tilt, dtype=np.float64)
+    B = box_vectors(box, tilt)
+    L_total = int(sum(ligand_sizes))
+    n_water = int(round((n_total - L_total) / 3.0))
+    centers = [np.zeros(3)]
+    for k in range(1, len(ligand_sizes)):
+        centers.append(centers[0] + np.asarray(displacements[0]))
+    lig_pos, lig_q, lig_s, lig_e = [], [], [], []
+    for k, Lk in enumerate(ligand_sizes):
+        lig_pos.append(_chain(rng, Lk) + centers[k])
+        q, sg, ep = _ligand_params(rng, Lk)
+        lig_q.append(q)
+        lig_s.append(sg)
+        lig_e.append(ep)
+    avoid = np.concatenate([np.concatenate([x, x + np.asarray(d)]) for x, d in zip(lig_pos, displacements)])
+    nside = int(math.ceil(n_water ** (1.0 / 3.0)))
+    while True:
+        g = (np.arange(nside) + 0.5) / nside
+        frac = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
+        sites = frac @ B
+        keep = np.ones(len(sites), dtype=bool)
+        for a_ in avoid:
+            d = min_image_triclinic(sites - a_, box, tilt)
+            keep &= (d * d).sum(axis=1) >= 0.3 * 0.3
+        if keep.sum() >= n_water:
+            break
+        nside += 1
+    sites = sites[keep]
+    chosen = np.sort(rng.choice(len(sites), size=n_water, replace=False))
+    O = sites[chosen] + rng.uniform(-0.02, 0.02, size=(n_water, 3))
+    half = math.radians(HOH_DEG) / 2.0
+    h_local = np.array([[R_OH * math.sin(half), R_OH * math.cos(half), 0.0],
+                        [-R_OH * math.sin(half), R_OH * math.cos(half), 0.0]])
+    n = 3 * n_water + L_total
+    pos = np.zeros((n, 3))
+    for w in range(n_water):
+        R = _rotation(rng)
+        pos[3 * w] = O[w]
+        pos[3 * w + 1] = O[w] + R @ h_local[0]
+        pos[3 * w + 2] = O[w] + R @ h_local[1]
+    q = np.zeros(n)
+    sig = np.zeros(n)
+    eps = np.zeros(n)
+    q[: 3 * n_water] = np.tile([WATER_O[0], WATER_H[0], WATER_H[0]], n_water)
+    sig[: 3 * n_water] = np.tile([WATER_O[1], WATER_H[1], WATER_H[1]], n_water)
+    eps[: 3 * n_water] = np.tile([WATER_O[2], WATER_H[2], WATER_H[2]], n_water)
+    ei, ej = [], []
+    base = np.arange(n_water) * 3
+    for a_, b_ in ((0, 1), (0, 2), (1, 2)):
+        ei.append(base + a_)
+        ej.append(base + b_)
+    displ = np.zeros((n, 3))
+    ligands = []
+    off = 3 * n_water
+    for k, Lk in enumerate(ligand_sizes):
+        idx = np.arange(off, off + Lk)
+        ligands.append(idx)
+        pos[idx] = lig_pos[k]
+        q[idx], sig[idx], eps[idx] = lig_q[k], lig_s[k], lig_e[k]
+        displ[idx] = np.asarray(displacements[k], dtype=np.float64)
+        for d in (1, 2):
+            ei.append(idx[:-d])
+            ej.append(idx[d:])
+        off += Lk
+    exc_i = np.concatenate(ei).astype(np.int32)
+    exc_j = np.concatenate(ej).astype(np.int32)
+    m = len(exc_i)
+    alpha, grid = 0.0, (0, 0, 0)
+    if method == PME:
+        alpha, grid = pme_parameters(cutoff, ewald_tol, box)
+    spec = NonbondedSpec(charge=q, sigma=sig, epsilon=eps, exc_i=exc_i, exc_j=exc_j, exc_qq=np.zeros(m),
+                         exc_sig=np.ones(m), exc_eps=np.zeros(m), method=method, cutoff=cutoff, box=box,
+                         eps_rf=eps_rf, ewald_tol=ewald_tol, alpha=alpha, grid=tuple(grid),
+                         tilt=tuple(float(t) for t in tilt))
+    if params is None:
+        params = default_params()
+    return ATMCase(spec=spec, pos=pos, displ=displ, params=np.asarray(params, dtype=np.float64), ligands=ligands,
+                   seed=seed, name=name)

@@ -913,6 +913,11 @@ bool MDDriver::check_lists() {
     // re-sort when the pair-tile count shows the atom order has decayed
     int tiles = 0;
     eng_->stats(&tiles, nullptr, nullptr);
+    // the baseline belongs to one list cutoff: a larger skin lists more tiles
+    if (base_skin_ != eng_->list_skin()) {
+        base_skin_ = eng_->list_skin();
+        base_tiles_ = 0;
+    }
     if (base_tiles_ == 0) base_tiles_ = tiles;
     bool due = opt_.reorder_interval > 0 ? step_ - last_reorder_step_ >= opt_.reorder_interval
                                          : tiles > base_tiles_ + base_tiles_ / 5;

@@ -138,7 +138,8 @@ private:
     bool forces_valid_ = false;
     bool have_positions_ = false;
     int reorders_ = 0;
-    int base_tiles_ = 0;
+    int base_tiles_ = 0;       // pair tiles after the last re-sort (at list skin base_skin_)
+    double base_skin_ = -1.0;
     long long last_reorder_step_ = 0;
     std::vector<int> in_off_;
     std::vector<int> dof_;  // per replica: 3 x moving atoms - constraints

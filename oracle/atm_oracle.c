@@ -55,6 +55,38 @@ static inline double min_image(double d, double L) { return d - L * floor(d / L 
 
 static int is_periodic(int method) { return method == ONB_CUTOFF_PERIODIC || method == ONB_PME; }
 
+static int is_triclinic(const onb_t* s) { return s->tilt[0] != 0.0 || s->tilt[1] != 0.0 || s->tilt[2] != 0.0; }
+
+/* The periodic shift that takes d to its minimum image (OpenMM's reduced-box
+ * rule: c, then b, then a), returned in shift (d - shift is the image). */
+static void image_shift(const onb_t* s, const double* d, double* shift) {
+    double v[3] = {d[0], d[1], d[2]};
+    double k = floor(v[2] / s->box[2] + 0.5);
+    v[0] -= k * s->tilt[1];
+    v[1] -= k * s->tilt[2];
+    v[2] -= k * s->box[2];
+    k = floor(v[1] / s->box[1] + 0.5);
+    v[0] -= k * s->tilt[0];
+    v[1] -= k * s->box[1];
+    k = floor(v[0] / s->box[0] + 0.5);
+    v[0] -= k * s->box[0];
+    for (int a = 0; a < 3; a++) shift[a] = d[a] - v[a];
+}
+
+/* Reciprocal box (rows r_i, as OpenMM's recipBoxVectors): the fractional
+ * coordinate along box vector d of position p is sum_i p_i r[i][d]. */
+static void recip_box(const onb_t* s, double r[3][3]) {
+    const double ax = s->box[0], by = s->box[1], cz = s->box[2];
+    const double bx = s->tilt[0], cx = s->tilt[1], cy = s->tilt[2];
+    memset(r, 0, 9 * sizeof(double));
+    r[0][0] = 1.0 / ax;
+    r[1][0] = -bx / (ax * by);
+    r[1][1] = 1.0 / by;
+    r[2][0] = (bx * cy - by * cx) / (ax * by * cz);
+    r[2][1] = -cy / (by * cz);
+    r[2][2] = 1.0 / cz;
+}
+
 /* Sorted CSR adjacency of exception partners, for the "is this pair an
  * exception" test of the pair loop. */
 typedef struct {
@@ -170,12 +202,17 @@ static inline double do_pair(const direct_job* J, int i, int j, double* fi_acc, 
     for (int a = 0; a < 3; a++) {
         dc[a] = J->pc[3 * j + a] - J->pc[3 * i + a];
         d[a] = J->pos[3 * j + a] - J->pos[3 * i + a];
-        if (per) {
-            /* the same image shift is applied to the evaluation geometry */
-            double shift = s->box[a] * floor(dc[a] / s->box[a] + 0.5);
-            dc[a] -= shift;
-            d[a] -= shift;
+    }
+    if (per) {
+        /* the same image shift is applied to the evaluation geometry */
+        double shift[3];
+        image_shift(s, dc, shift);
+        for (int a = 0; a < 3; a++) {
+            dc[a] -= shift[a];
+            d[a] -= shift[a];
         }
+    }
+    for (int a = 0; a < 3; a++) {
         r2c += dc[a] * dc[a];
         r2 += d[a] * d[a];
     }
@@ -218,7 +255,7 @@ static double direct_space(const direct_job* J) {
     const onb_t* s = J->s;
     int n = s->n;
     double energy = 0.0;
-    int use_cells = is_periodic(s->method);
+    int use_cells = is_periodic(s->method) && !is_triclinic(s);
     int nc[3] = {1, 1, 1};
     if (use_cells) {
         for (int a = 0; a < 3; a++) {
@@ -336,9 +373,10 @@ static double exceptions_term(const onb_t* s, const double* pos, double* forces,
             fr += f;
         }
         if (s->method == ONB_PME) {
-            double dm[3], r2m = 0.0;
+            double dm[3], sh[3], r2m = 0.0;
+            image_shift(s, d, sh);
             for (int a = 0; a < 3; a++) {
-                dm[a] = min_image(d[a], s->box[a]);
+                dm[a] = d[a] - sh[a];
                 r2m += dm[a] * dm[a];
             }
             double r = sqrt(r2m);
@@ -575,19 +613,22 @@ static double pme_solve(const onb_t* s, double* grid /* complex, in: Q, out: phi
     double vol = s->box[0] * s->box[1] * s->box[2];
     double pref = ONB_ONE_4PI_EPS0 / (M_PI * vol);
     double fac = M_PI * M_PI / (s->alpha * s->alpha);
+    double rb[3][3];
+    recip_box(s, rb);
     double energy = 0.0;
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(g_threads) reduction(+ : energy)
 #endif
     for (int ix = 0; ix < Kx; ix++) {
         int mxi = ix <= Kx / 2 ? ix : ix - Kx;
-        double kx = mxi / s->box[0];
         for (int iy = 0; iy < Ky; iy++) {
             int myi = iy <= Ky / 2 ? iy : iy - Ky;
-            double ky = myi / s->box[1];
             for (int iz = 0; iz < Kz; iz++) {
                 int mzi = iz <= Kz / 2 ? iz : iz - Kz;
-                double kz = mzi / s->box[2];
+                /* m = mx a* + my b* + mz c*, the reciprocal vectors being the columns of rb */
+                double kx = mxi * rb[0][0];
+                double ky = mxi * rb[1][0] + myi * rb[1][1];
+                double kz = mxi * rb[2][0] + myi * rb[2][1] + mzi * rb[2][2];
                 long idx = ((long)ix * Ky + iy) * Kz + iz;
                 double m2 = kx * kx + ky * ky + kz * kz;
                 double G = 0.0;
@@ -612,8 +653,10 @@ typedef struct {
 } stencil_t;
 
 static void atom_stencil(const onb_t* s, const double* p, stencil_t* st) {
+    double rb[3][3];
+    recip_box(s, rb);
     for (int a = 0; a < 3; a++) {
-        double f = p[a] / s->box[a];
+        double f = p[0] * rb[0][a] + p[1] * rb[1][a] + p[2] * rb[2][a];
         f -= floor(f);
         double u = f * s->grid[a];
         int b = (int)floor(u);
@@ -672,9 +715,12 @@ static double pme_recip(const onb_t* s, const double* pos, double* forces, doubl
                 }
             }
             if (forces) {
-                forces[3 * i + 0] -= q * gx * Kx / s->box[0];
-                forces[3 * i + 1] -= q * gy * Ky / s->box[1];
-                forces[3 * i + 2] -= q * gz * Kz / s->box[2];
+                /* -q grad phi: d(grid coordinate d)/dx_j = K_d rb[j][d] */
+                double rb[3][3];
+                recip_box(s, rb);
+                const double g[3] = {gx * Kx, gy * Ky, gz * Kz};
+                for (int j = 0; j < 3; j++)
+                    forces[3 * i + j] -= q * (g[0] * rb[j][0] + g[1] * rb[j][1] + g[2] * rb[j][2]);
             }
             if (dUdq) dUdq[i] += phi;
         }
@@ -685,6 +731,8 @@ static double pme_recip(const onb_t* s, const double* pos, double* forces, doubl
 
 int onb_ewald_recip_exact(const onb_t* s, const double* pos, int kmax, double* energy, double* forces) {
     double vol = s->box[0] * s->box[1] * s->box[2];
+    double rb[3][3];
+    recip_box(s, rb);
     double fac = M_PI * M_PI / (s->alpha * s->alpha);
     double e = 0.0;
     if (forces) memset(forces, 0, sizeof(double) * 3 * (size_t)s->n);
@@ -694,7 +742,8 @@ int onb_ewald_recip_exact(const onb_t* s, const double* pos, int kmax, double* e
         for (int my = -kmax; my <= kmax; my++)
             for (int mz = -kmax; mz <= kmax; mz++) {
                 if (mx == 0 && my == 0 && mz == 0) continue;
-                double k[3] = {mx / s->box[0], my / s->box[1], mz / s->box[2]};
+                double k[3] = {mx * rb[0][0], mx * rb[1][0] + my * rb[1][1],
+                               mx * rb[2][0] + my * rb[2][1] + mz * rb[2][2]};
                 double m2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
                 double f = exp(-fac * m2) / m2;
                 double sr = 0.0, si = 0.0;

@@ -16,7 +16,10 @@
  *     exclusions and exceptions, following the NonbondedForce definitions in
  *     OpenMM's user guide (theory chapter).
  *
- * Units: nm, kJ/mol, elementary charges.  Boxes are orthorhombic.
+ * Units: nm, kJ/mol, elementary charges.  Periodic boxes are OpenMM's reduced
+ * triclinic form a = (box[0], 0, 0), b = (tilt[0], box[1], 0), c = (tilt[1],
+ * tilt[2], box[2]) (orthorhombic when the tilts are zero), with OpenMM's minimum
+ * image: subtract c, then b, then a, each rounded to the nearest multiple.
  */
 #ifndef ATM_ORACLE_H
 #define ATM_ORACLE_H
@@ -47,7 +50,8 @@ typedef struct {
     int grid[3];                             /* PME grid */
     int order;                               /* PME B-spline order */
     int use_disp_corr;                       /* long-range LJ correction */
-    double box[3];                           /* orthorhombic edges, nm */
+    double box[3];                           /* diagonal of the box vectors, nm */
+    double tilt[3];                          /* b_x, c_x, c_y of the box vectors, nm */
 } onb_t;
 
 typedef struct {

@@ -10,7 +10,9 @@ NonbondedForce evaluation the reference delegates to OpenMM
 
 A "spec" is any object with the attributes charge, sigma, epsilon (arrays),
 exc_i, exc_j, exc_qq, exc_sig, exc_eps (arrays), method, cutoff, eps_rf, alpha,
-grid (3 ints), order, use_disp_corr, box (3 floats).
+grid (3 ints), order, use_disp_corr, box (3 floats: the diagonal of the box
+vectors) and optionally tilt (b_x, c_x, c_y of OpenMM's reduced triclinic box
+vectors a = (box0, 0, 0), b = (b_x, box1, 0), c = (c_x, c_y, box2)).
 """
 from __future__ import annotations
 
@@ -45,6 +47,7 @@ class _ONB(C.Structure):
         ("order", C.c_int),
         ("use_disp_corr", C.c_int),
         ("box", C.c_double * 3),
+        ("tilt", C.c_double * 3),
     ]
 
 
@@ -118,9 +121,11 @@ class _Pinned:
         o.cutoff = float(spec.cutoff)
         o.eps_rf = float(spec.eps_rf)
         o.alpha = float(spec.alpha)
+        tilt = getattr(spec, "tilt", None)
         for a in range(3):
             o.grid[a] = int(spec.grid[a])
             o.box[a] = float(spec.box[a])
+            o.tilt[a] = float(tilt[a]) if tilt is not None else 0.0
         o.order = int(spec.order)
         o.use_disp_corr = int(spec.use_disp_corr)
         self.struct = o

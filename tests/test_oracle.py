@@ -208,3 +208,70 @@ def test_threads_do_not_change_results():
     O.set_threads(1)
     assert E4 == pytest.approx(E1, rel=1e-12)
     np.testing.assert_allclose(F4, F1, rtol=1e-9, atol=1e-9)
+
+
+# ---------------------------------------------------------------------------
+# Triclinic boxes (OpenMM's reduced form a = (ax,0,0), b = (bx,by,0), c = (cx,cy,cz))
+# ---------------------------------------------------------------------------
+
+TILTS = [(0.9, -0.7, 0.8), (1.4, 1.3, -1.2)]
+
+
+@pytest.mark.parametrize("tilt", TILTS)
+def test_triclinic_pme_matches_exact_ewald(tilt):
+    import copy
+
+    c = S.triclinic_water_ligand_box(3000, (3.2, 3.0, 2.9), tilt, [14], [(1.3, 1.2, 1.1)], S.PME, 0.9, seed=5)
+    fine = copy.copy(c.spec)
+    fine.grid = tuple(2 * g for g in c.spec.grid)
+    E_pme = O.nonbonded(fine, c.pos, forces=False)[2]["recip"]
+    E_exact, _ = O.ewald_recip_exact(c.spec, c.pos, 16)
+    assert abs(E_pme - E_exact) < 0.05, (E_pme, E_exact)
+
+
+@pytest.mark.parametrize("method", [S.PME, S.CUTOFF_PERIODIC])
+def test_triclinic_forces_are_energy_gradients(method):
+    c = S.triclinic_water_ligand_box(600, (2.1, 2.0, 1.95), (0.7, -0.6, 0.5), [8], [(0.9, 0.8, 0.7)], method, 0.9,
+                                     seed=6)
+    E, F, _ = O.nonbonded(c.spec, c.pos)
+    h = 1e-5
+    rng = np.random.default_rng(0)
+    for i in rng.choice(c.n, 6, replace=False):
+        for d in range(3):
+            p1, p2 = c.pos.copy(), c.pos.copy()
+            p1[i, d] += h
+            p2[i, d] -= h
+            # the pair set stays that of the unperturbed geometry
+            fd = -(O.nonbonded(c.spec, p1, pos_cut=c.pos, forces=False)[0] -
+                   O.nonbonded(c.spec, p2, pos_cut=c.pos, forces=False)[0]) / (2 * h)
+            assert abs(F[i, d] - fd) <= 1e-5 * max(1.0, abs(fd)), (i, d, F[i, d], fd)
+
+
+def test_triclinic_direct_space_matches_image_search():
+    """Reaction field over the pairs within the cutoff, the pair vector being the
+    shortest over the 125 images next to the reduced-form minimum image."""
+    c = S.triclinic_water_ligand_box(900, (2.3, 2.2, 2.1), (0.9, -0.8, 0.7), [8], [(1.0, 0.9, 0.8)],
+                                     S.CUTOFF_PERIODIC, 0.9, seed=7)
+    sp = c.spec
+    _, _, T = O.nonbonded(sp, c.pos, forces=False)
+    B = S.box_vectors(sp.box, sp.tilt)
+    shifts = np.array([(i, j, k) for i in range(-2, 3) for j in range(-2, 3) for k in range(-2, 3)]) @ B
+    excl = set(zip(sp.exc_i.tolist(), sp.exc_j.tolist())) | set(zip(sp.exc_j.tolist(), sp.exc_i.tolist()))
+    rc, er = sp.cutoff, sp.eps_rf
+    krf = (er - 1) / ((2 * er + 1) * rc ** 3)
+    crf = 3 * er / ((2 * er + 1) * rc)
+    E = 0.0
+    for i in range(c.n):
+        d = c.pos[i + 1:] - c.pos[i]
+        dd = d[:, None, :] + shifts[None, :, :]
+        r2 = (dd * dd).sum(-1).min(axis=1)
+        for jj in np.nonzero(r2 < rc * rc)[0]:
+            j = i + 1 + jj
+            if (i, j) in excl:
+                continue
+            r = np.sqrt(r2[jj])
+            sig = 0.5 * (sp.sigma[i] + sp.sigma[j])
+            eps = np.sqrt(sp.epsilon[i] * sp.epsilon[j])
+            s6 = (sig / r) ** 6
+            E += 4 * eps * (s6 * s6 - s6) + O.ONE_4PI_EPS0 * sp.charge[i] * sp.charge[j] * (1 / r + krf * r * r - crf)
+    assert abs(T["direct"] - E) <= 1e-8 * max(1.0, abs(E)), (T["direct"], E)
