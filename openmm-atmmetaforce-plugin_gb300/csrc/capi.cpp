@@ -457,20 +457,29 @@ int atm_system_get_num_particles(atm_system_t sys, int* n) {
     API_END
 }
 
-static void read_box(const double* a, const double* b, const double* c, double* box) {
+// Box vectors in OpenMM's reduced form (System::setDefaultPeriodicBoxVectors):
+// a = (ax, 0, 0), b = (bx, by, 0), c = (cx, cy, cz) with ax, by, cz > 0,
+// |bx| <= ax/2, |cx| <= ax/2, |cy| <= by/2.  box = (ax, by, cz), tilt = (bx, cx, cy).
+static void read_box(const double* a, const double* b, const double* c, double* box, double* tilt) {
     REQUIRE(a && b && c, ATM_ERR_INVALID_ARGUMENT, "null box vector");
-    REQUIRE(a[1] == 0 && a[2] == 0 && b[0] == 0 && b[2] == 0 && c[0] == 0 && c[1] == 0, ATM_ERR_UNSUPPORTED,
-            "Only rectangular periodic boxes are supported");
+    REQUIRE(a[1] == 0 && a[2] == 0 && b[2] == 0, ATM_ERR_INVALID_ARGUMENT,
+            "First periodic box vector must be parallel to x, the second must lie in the xy plane");
     REQUIRE(a[0] > 0 && b[1] > 0 && c[2] > 0, ATM_ERR_INVALID_ARGUMENT, "Box vectors must be positive");
+    REQUIRE(std::fabs(b[0]) <= 0.5 * a[0] * (1 + 1e-12) && std::fabs(c[0]) <= 0.5 * a[0] * (1 + 1e-12) &&
+                std::fabs(c[1]) <= 0.5 * b[1] * (1 + 1e-12),
+            ATM_ERR_INVALID_ARGUMENT, "Triclinic box vectors must be in reduced form");
     box[0] = a[0];
     box[1] = b[1];
     box[2] = c[2];
+    tilt[0] = b[0];
+    tilt[1] = c[0];
+    tilt[2] = c[1];
 }
 
 int atm_system_set_default_periodic_box_vectors(atm_system_t sys, const double* a, const double* b, const double* c) {
     API_BEGIN
     REQUIRE(sys, ATM_ERR_INVALID_ARGUMENT, "null system");
-    read_box(a, b, c, sys->sys.box);
+    read_box(a, b, c, sys->sys.box, sys->sys.tilt);
     API_END
 }
 
@@ -619,9 +628,9 @@ int atm_context_set_positions(atm_context_t ctx, const double* pos, int n) {
 int atm_context_set_periodic_box_vectors(atm_context_t ctx, const double* a, const double* b, const double* c) {
     API_BEGIN
     REQUIRE(ctx, ATM_ERR_INVALID_ARGUMENT, "null context");
-    double box[3];
-    read_box(a, b, c, box);
-    ctx->eng->set_box(0, box);
+    double box[3], tilt[3];
+    read_box(a, b, c, box, tilt);
+    ctx->eng->set_box(0, box, tilt);
     ctx->dirty = true;
     API_END
 }
@@ -738,9 +747,9 @@ int atm_batch_set_parameter(atm_batch_t b, int replica, const char* name, double
 int atm_batch_set_periodic_box_vectors(atm_batch_t b, int replica, const double* a, const double* b_, const double* c) {
     API_BEGIN
     REQUIRE(b, ATM_ERR_INVALID_ARGUMENT, "null batch");
-    double box[3];
-    read_box(a, b_, c, box);
-    b->eng->set_box(replica, box);
+    double box[3], tilt[3];
+    read_box(a, b_, c, box, tilt);
+    b->eng->set_box(replica, box, tilt);
     API_END
 }
 

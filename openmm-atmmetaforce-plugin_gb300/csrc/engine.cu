@@ -71,7 +71,10 @@ ReplicaSpec spec_from_system(const System& sys) {
     s.cutoff = nb.cutoff;
     s.epsRF = nb.epsRF;
     s.dispersion = nb.dispersionCorrection;
-    for (int a = 0; a < 3; a++) s.box[a] = sys.box[a];
+    for (int a = 0; a < 3; a++) {
+        s.box[a] = sys.box[a];
+        s.tilt[a] = sys.tilt[a];
+    }
     if (nb.method == NonbondedForce::PME) {
         if (nb.alpha > 0 && nb.grid[0] > 0 && nb.grid[1] > 0 && nb.grid[2] > 0) {
             s.alpha = nb.alpha;
@@ -270,14 +273,17 @@ void Engine::set_all_positions(const double* pos) {
     std::memcpy(h_pos_, pos, sizeof(double) * 3 * (size_t)n_in_);
 }
 
-void Engine::set_box(int r, const double* box) {
+void Engine::set_box(int r, const double* box, const double* tilt) {
     if (r < 0 || r >= R_) throw Error(2, "Replica index out of range");
     if (periodic_)
         for (int a = 0; a < 3; a++)
             if (!(box[a] >= 2.0 * (cutoff_ + skin_)))
                 throw Error(1,
                             "The periodic box must be at least twice the cutoff (plus the list skin) in every dimension");
-    for (int a = 0; a < 3; a++) specs_[r].box[a] = box[a];
+    for (int a = 0; a < 3; a++) {
+        specs_[r].box[a] = box[a];
+        specs_[r].tilt[a] = tilt ? tilt[a] : 0.0;
+    }
     force_build_ = true;  // periodic images move with the box
     infl_dirty_ = true;
 }
@@ -288,7 +294,11 @@ void Engine::update_influence(cudaStream_t st) {
     if (!use_fft_ || method_ != NonbondedForce::PME) return;
     for (int r = 0; r < R_; r++) {
         const RepDev& rd = rep_host_[r];
-        launch_influence(A_.influence + rd.cplx_off / 2, A_.moduli, rd.mod_off, rd.K, specs_[r].box, alpha_, st);
+        const ReplicaSpec& s = specs_[r];
+        double rb[6];
+        recip_box(s, rb);
+        launch_influence(A_.influence + rd.cplx_off / 2, A_.moduli, rd.mod_off, rd.K, rb,
+                         s.box[0] * s.box[1] * s.box[2], alpha_, st);
     }
     CUDA_CHECK(cudaGetLastError());
 }
@@ -338,7 +348,42 @@ void Engine::set_box_constants(RepDev& rd, const ReplicaSpec& s) const {
         rd.ibox[a] = periodic_ ? (float)(1.0 / L) : 0.0f;
         rd.boxd[a] = L;
         rd.iboxd[a] = periodic_ ? 1.0 / L : 0.0;
+        const double t = periodic_ ? s.tilt[a] : 0.0;
+        rd.tiltd[a] = t;
+        rd.tilt[a] = (float)t;
     }
+    rd.tiltd[3] = 0.0;
+    rd.tilt[3] = 0.0f;
+    rd.tric = (rd.tiltd[0] != 0.0 || rd.tiltd[1] != 0.0 || rd.tiltd[2] != 0.0) ? 1 : 0;
+    double r[6];
+    recip_box(s, r);
+    for (int k = 0; k < 6; k++) rd.recip[k] = periodic_ ? (float)r[k] : 0.0f;
+    rd.recip[6] = rd.recip[7] = 0.0f;
+    rd.wmin = periodic_ ? (float)min_face_distance(s) : 1.0e30f;
+}
+
+// Reciprocal box of a replica (rows, lower triangular): r00, r10, r11, r20, r21,
+// r22; the fractional coordinate along box vector d of p is sum_i p_i r[i][d].
+void Engine::recip_box(const ReplicaSpec& s, double* r) {
+    const double ax = s.box[0], by = s.box[1], cz = s.box[2];
+    const double bx = s.tilt[0], cx = s.tilt[1], cy = s.tilt[2];
+    r[0] = 1.0 / ax;
+    r[1] = -bx / (ax * by);
+    r[2] = 1.0 / by;
+    r[3] = (bx * cy - by * cx) / (ax * by * cz);
+    r[4] = -cy / (by * cz);
+    r[5] = 1.0 / cz;
+}
+
+// Smallest distance between opposite faces: V / |b x c|, V / |a x c|, V / |a x b|.
+double Engine::min_face_distance(const ReplicaSpec& s) {
+    const double ax = s.box[0], by = s.box[1], cz = s.box[2];
+    const double bx = s.tilt[0], cx = s.tilt[1], cy = s.tilt[2];
+    const double V = ax * by * cz;
+    const double bc = std::sqrt(by * cz * by * cz + bx * cz * bx * cz + (bx * cy - by * cx) * (bx * cy - by * cx));
+    const double ac = ax * std::sqrt(cy * cy + cz * cz);
+    const double ab = ax * by;
+    return std::min(V / bc, std::min(V / ac, V / ab));
 }
 
 // Squared cutoffs of the pair kernel and of the list builds (NoCutoff: every pair;
@@ -424,14 +469,23 @@ void Engine::build_layout() {
                 }
             for (int a = 0; a < 3; a++) span[a] = std::max(hi[a] - lo[a], 1e-6) * (1.0 + 1e-9);
         }
+        double rb[6];
+        recip_box(s, rb);
         for (auto& kv : mol) {
             int i = kv.second[0];
             uint32_t c[3];
+            const double* p = pos + 3 * (size_t)i;
+            // periodic: fractional coordinates along the box vectors, wrapped
+            const double fr[3] = {p[0] * rb[0] + p[1] * rb[1] + p[2] * rb[3], p[1] * rb[2] + p[2] * rb[4],
+                                  p[2] * rb[5]};
             for (int a = 0; a < 3; a++) {
-                double L = span[a];
-                double x = pos[3 * i + a] - lo[a];
-                if (periodic_) x -= L * std::floor(x / L);
-                long v = (long)(x / L * (1 << bits));
+                double x;
+                if (periodic_) {
+                    x = fr[a] - std::floor(fr[a]);
+                } else {
+                    x = (p[a] - lo[a]) / span[a];
+                }
+                long v = (long)(x * (1 << bits));
                 c[a] = (uint32_t)std::min(std::max(v, 0L), (long)(1 << bits) - 1);
             }
             keys.push_back({hilbert3(c[0], c[1], c[2], bits), kv.first});
@@ -683,6 +737,7 @@ void Engine::build_layout() {
     }
     groups_.clear();
     fft_tw_.clear();
+    fft_stages_.clear();
     fft_plane_.clear();
     fft_conv_.clear();
     use_fft_ = false;
@@ -723,6 +778,7 @@ void Engine::build_layout() {
                     const double t = -2.0 * kPi * k / rd.K[a];
                     fft_tw_.push_back(make_float2((float)std::cos(t), (float)std::sin(t)));
                 }
+                rd.fft_plan[a] = fft_plan_stages(rd.K[a], fft_stages_);
             }
         }
         build_bricks();
@@ -963,6 +1019,7 @@ void Engine::alloc_device() {
     a.posq = dalloc<float4>(d_allocs_, NA_);
     a.posq2 = full_ ? dalloc<float4>(d_allocs_, NA_) : nullptr;
     a.posq_ref = dalloc<float4>(d_allocs_, NA_);
+    a.rep_hmax = dalloc<unsigned>(d_allocs_, R_);
     a.list_counts = d_counts_;
     {
         int* ctl = dalloc<int>(d_allocs_, 2);
@@ -1020,6 +1077,7 @@ void Engine::alloc_device() {
         a.moduli = dupload(d_allocs_, moduli_);
         a.use_fft = use_fft_ ? 1 : 0;
         a.fft_tw = dupload(d_allocs_, fft_tw_);
+        a.fft_stages = dupload(d_allocs_, fft_stages_);
         a.fft_plane_ctas = (int)fft_plane_.size();
         a.fft_plane = dupload(d_allocs_, fft_plane_);
         a.fft_plane_smem = fft_plane_smem_;
@@ -1070,6 +1128,13 @@ void Engine::update_rep_table() {
     }
     std::memcpy(h_reps_, rep_host_.data(), sizeof(RepDev) * (size_t)R_);
     *h_beta_ = beta_;
+    // the finder's variant (orthorhombic or triclinic) is part of the recorded graphs
+    int tric = 0;
+    for (int r = 0; r < R_; r++) tric |= rep_host_[r].tric;
+    if (tric != A_.any_tric) {
+        A_.any_tric = tric;
+        destroy_graphs();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1101,6 +1166,7 @@ void Engine::record(cudaStream_t st, bool host_io) {
     CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
     launch_prepare(a, st);
     launch_decide(a, st);
     bool pme = method_ == NonbondedForce::PME;
@@ -1232,6 +1298,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
             mark("start");
             launch_prepare(a, st);
             launch_decide(a, st);
@@ -1391,6 +1458,10 @@ void Engine::launch_device(const double* d_pos, cudaStream_t stream) {
         return;
     }
     update_rep_table();
+    if (!graph_dev_) {  // the box changed between orthorhombic and triclinic
+        run_device(d_pos, stream);
+        return;
+    }
     update_influence(stream);
     // the control word stays as the last synchronous evaluation left it: 0 with a
     // skin (the device decides), 1 without one (every evaluation builds)

@@ -25,6 +25,7 @@ struct ReplicaSpec {
     int grid[3] = {0, 0, 0};
     bool dispersion = false;
     double box[3] = {0, 0, 0};
+    double tilt[3] = {0, 0, 0};  // b_x, c_x, c_y (OpenMM's reduced triclinic box vectors)
     double params[NUM_GLOBALS] = {0};
     bool var_nb = true;
 };
@@ -54,7 +55,7 @@ public:
 
     void set_positions(int r, const double* pos);
     void set_all_positions(const double* pos);
-    void set_box(int r, const double* box);
+    void set_box(int r, const double* box, const double* tilt = nullptr);
     void set_param(int r, int which, double v);
     double param(int r, int which) const { return specs_[r].params[which]; }
     void set_displacements(int r, const double* displ);  // 3n, particle count unchanged
@@ -94,6 +95,7 @@ public:
     const double* results_device() const { return A_.results; }
     const double* matrix_device() const { return A_.matrix; }
     const double* box(int r) const { return specs_[r].box; }
+    const double* tilt(int r) const { return specs_[r].tilt; }
     // Re-sort from device positions at the next evaluation (the layout, tile
     // rows and exclusion masks are rebuilt; results do not change).
     void reorder_from_device(const double* d_pos, cudaStream_t stream);
@@ -128,6 +130,8 @@ public:
 private:
     void build_layout();
     void set_box_constants(RepDev& rd, const ReplicaSpec& s) const;
+    static void recip_box(const ReplicaSpec& s, double* r);
+    static double min_face_distance(const ReplicaSpec& s);
     float cutoff2() const;
     float list_cutoff2() const;
     void build_bricks();
@@ -203,6 +207,7 @@ private:
     // hand-written transforms: used when every grid plane fits in shared memory
     bool use_fft_ = false;
     std::vector<float2> fft_tw_;
+    std::vector<FftStage> fft_stages_;
     std::vector<int2> fft_plane_;
     std::vector<int4> fft_conv_;
     int fft_plane_smem_ = 0, fft_conv_smem_ = 0;

@@ -45,9 +45,7 @@ __device__ __forceinline__ void warp_bbox(float x, float y, float z, const RepDe
                                           int lane, int nreal) {
     float x0 = __shfl_sync(FULL_MASK, x, 0), y0 = __shfl_sync(FULL_MASK, y, 0), z0 = __shfl_sync(FULL_MASK, z, 0);
     float dx = x - x0, dy = y - y0, dz = z - z0;
-    dx -= R.box[0] * rintf(dx * R.ibox[0]);
-    dy -= R.box[1] * rintf(dy * R.ibox[1]);
-    dz -= R.box[2] * rintf(dz * R.ibox[2]);
+    min_image3(dx, dy, dz, R);
     float lx = dx, ly = dy, lz = dz, hx = dx, hy = dy, hz = dz;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -75,17 +73,16 @@ __global__ void k_prepare(Args a) {
     const int nreal = __popc(__ballot_sync(FULL_MASK, o >= 0));  // padding sits at the end of a block
     if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
     const double* p = a.pos_in + 3 * (size_t)(R.in_off + o);
-    float x = (float)(p[0] - R.boxd[0] * floor(p[0] * R.iboxd[0]));
-    float y = (float)(p[1] - R.boxd[1] * floor(p[1] * R.iboxd[1]));
-    float z = (float)(p[2] - R.boxd[2] * floor(p[2] * R.iboxd[2]));
+    double xd = p[0], yd = p[1], zd = p[2];
+    wrap3d(xd, yd, zd, R);  // FP64 wrap into the unit cell
+    float x = (float)xd, y = (float)yd, z = (float)zd;
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
     if (a.skin_half2 > 0.f) {
         // displacement since the last list build (minimum image: wrapping is no motion)
         const float4 r = a.posq_ref[s];
-        const float dx = x - r.x - R.box[0] * rintf((x - r.x) * R.ibox[0]);
-        const float dy = y - r.y - R.box[1] * rintf((y - r.y) * R.ibox[1]);
-        const float dz = z - r.z - R.box[2] * rintf((z - r.z) * R.ibox[2]);
+        float dx = x - r.x, dy = y - r.y, dz = z - r.z;
+        min_image3(dx, dy, dz, R);
         float d2 = dx * dx + dy * dy + dz * dz;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(FULL_MASK, d2, o));
@@ -96,13 +93,20 @@ __global__ void k_prepare(Args a) {
     if (a.adjoint)
         for (int k = 0; k < 3; k++) a.D[(size_t)k * a.NA + s] = 0ull;
     warp_bbox(x, y, z, R, &a.bb_c[b], &a.bb_h[b], lane, nreal);
+    if (R.tric && lane == 0) {  // (lane 0 wrote the box)
+        const float4 h = a.bb_h[b];
+        atomicMax(&a.rep_hmax[rep], __float_as_uint(sqrtf(h.x * h.x + h.y * h.y + h.z * h.z)));
+    }
     if (a.full) {
         float4 d = a.displ[s];
-        float x2 = wrapf(x + d.x, R.box[0], R.ibox[0]);
-        float y2 = wrapf(y + d.y, R.box[1], R.ibox[1]);
-        float z2 = wrapf(z + d.z, R.box[2], R.ibox[2]);
+        float x2 = x + d.x, y2 = y + d.y, z2 = z + d.z;
+        wrap3(x2, y2, z2, R);
         a.posq2[s] = make_float4(x2, y2, z2, q);
         warp_bbox(x2, y2, z2, R, &a.bb_c2[b], &a.bb_h2[b], lane, nreal);
+        if (R.tric && lane == 0) {
+            const float4 h = a.bb_h2[b];
+            atomicMax(&a.rep_hmax[rep], __float_as_uint(sqrtf(h.x * h.x + h.y * h.y + h.z * h.z)));
+        }
     }
     if (b == 0 && lane == 0) a.status->next_tile = 0;
 }
@@ -172,9 +176,8 @@ __device__ __forceinline__ double exc_term(const Args& a, const RepDev& R, const
     f[2] = fr * dz;
     if (a.method == 4) {
         // Ewald exclusion correction at the minimum-image separation
-        double mx = dx - R.boxd[0] * rint(dx * R.iboxd[0]);
-        double my = dy - R.boxd[1] * rint(dy * R.iboxd[1]);
-        double mz = dz - R.boxd[2] * rint(dz * R.iboxd[2]);
+        double mx = dx, my = dy, mz = dz;
+        min_image3d(mx, my, mz, R);
         double m2 = mx * mx + my * my + mz * mz;
         if (m2 > 0.0) {
             double r = sqrt(m2);
@@ -217,9 +220,8 @@ __device__ __forceinline__ float exc_term_f(const Args& a, const RepDev& R, cons
     f[2] = fr * dz;
     if (a.method == 4) {
         float pw = (float)p.w;
-        float mx = dx - R.box[0] * rintf(dx * R.ibox[0]);
-        float my = dy - R.box[1] * rintf(dy * R.ibox[1]);
-        float mz = dz - R.box[2] * rintf(dz * R.ibox[2]);
+        float mx = dx, my = dy, mz = dz;
+        min_image3(mx, my, mz, R);
         float m2 = mx * mx + my * my + mz * mz;
         if (m2 > 0.0f) {
             float r = sqrtf(m2);
@@ -356,10 +358,11 @@ struct Stencil {
 };
 
 __device__ __forceinline__ void make_stencil(float x, float y, float z, const RepDev& R, Stencil& S, bool deriv) {
-    float c[3] = {x, y, z};
+    float fr[3];
+    frac3(x, y, z, R, fr);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        float f = c[d] * R.ibox[d];
+        float f = fr[d];
         f -= floorf(f);
         float u = f * (float)R.K[d];
         int b = (int)floorf(u);
@@ -390,11 +393,11 @@ constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kBrickPad = kOrder - 1;      // stencil reach below and above a brick
 constexpr float kGridScale = 33554432.0f;  // 2^25 fixed-point units per e
 
-// Does the cyclic range of base indices of a box (centre c, half extent h, nm)
-// meet the cyclic interval [o, o + len) of Z_K?
-__device__ __forceinline__ bool cyc_meet(float c, float h, float iL, int K, int o, int len) {
-    const int lo = (int)floorf((c - h) * iL * (float)K) - 1;
-    const int n = (int)floorf((c + h) * iL * (float)K) + 1 - lo + 1;
+// Does the cyclic range of base indices of a box (fractional centre fc and half
+// width fh along one box vector) meet the cyclic interval [o, o + len) of Z_K?
+__device__ __forceinline__ bool cyc_meet(float fc, float fh, int K, int o, int len) {
+    const int lo = (int)floorf((fc - fh) * (float)K) - 1;
+    const int n = (int)floorf((fc + fh) * (float)K) + 1 - lo + 1;
     if (n >= K) return true;
     int A = lo % K;
     if (A < 0) A += K;
@@ -405,10 +408,16 @@ __device__ __forceinline__ bool cyc_meet(float c, float h, float iL, int K, int 
     return d1 < n || d2 < len;
 }
 
+// A block's bounding box (centre c, half extents h, nm) in fractional coordinates:
+// centre p . r_d, half width sum_i h_i |r[i][d]| (r the reciprocal box).
 __device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev& R, const int* o, const int* e) {
-    return cyc_meet(c.x, h.x, R.ibox[0], R.K[0], o[0], e[0] + kOrder - 1) &&
-           cyc_meet(c.y, h.y, R.ibox[1], R.K[1], o[1], e[1] + kOrder - 1) &&
-           cyc_meet(c.z, h.z, R.ibox[2], R.K[2], o[2], e[2] + kOrder - 1);
+    float f[3];
+    frac3(c.x, c.y, c.z, R, f);
+    const float w0 = h.x * fabsf(R.recip[0]) + h.y * fabsf(R.recip[1]) + h.z * fabsf(R.recip[3]);
+    const float w1 = h.y * fabsf(R.recip[2]) + h.z * fabsf(R.recip[4]);
+    const float w2 = h.z * fabsf(R.recip[5]);
+    return cyc_meet(f[0], w0, R.K[0], o[0], e[0] + kOrder - 1) && cyc_meet(f[1], w1, R.K[1], o[1], e[1] + kOrder - 1) &&
+           cyc_meet(f[2], w2, R.K[2], o[2], e[2] + kOrder - 1);
 }
 
 constexpr int kSpreadChunk = kBrickThreads;  // blocks examined per pass (one per thread)
@@ -441,17 +450,19 @@ __device__ __forceinline__ void spread_candidates(const Args& a, const RepDev& R
         if (code == 1) p.w = -p.w;
         if (code == 3) {
             const float4 dd = a.displ[s];
-            p.x = wrapf(p.x + dd.x, R.box[0], R.ibox[0]);
-            p.y = wrapf(p.y + dd.y, R.box[1], R.ibox[1]);
-            p.z = wrapf(p.z + dd.z, R.box[2], R.ibox[2]);
+            p.x += dd.x;
+            p.y += dd.y;
+            p.z += dd.z;
+            wrap3(p.x, p.y, p.z, R);
         }
         bool ok = lane < nreal && p.w != 0.0f;
         int lb[3];
         if (ok) {
-            const float cc[3] = {p.x, p.y, p.z};
+            float cc[3];
+            frac3(p.x, p.y, p.z, R, cc);
 #pragma unroll
             for (int d = 0; d < 3; d++) {
-                float f = cc[d] * R.ibox[d];
+                float f = cc[d];
                 f -= floorf(f);
                 int bs = (int)floorf(f * (float)R.K[d]);
                 if (bs >= R.K[d]) bs -= R.K[d];
@@ -647,7 +658,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv(Args a) {
         int ix = (int)(rem / Ky);
         int mxi = ix <= Kx / 2 ? ix : ix - Kx;
         int myi = iy <= Ky / 2 ? iy : iy - Ky;
-        float kx = mxi * R.ibox[0], ky = myi * R.ibox[1], kz = iz * R.ibox[2];
+        // m = mx a* + my b* + mz c* (the reciprocal vectors are the columns of the reciprocal box)
+        float kx = mxi * R.recip[0], ky = fmaf(myi, R.recip[2], mxi * R.recip[1]),
+              kz = fmaf(iz, R.recip[5], fmaf(myi, R.recip[4], mxi * R.recip[3]));
         float m2 = kx * kx + ky * ky + kz * kz;
         float G = (k == 0) ? 0.0f : pref * expf(-fac * m2) / (m2 * mx[ix] * my[iy] * mz[iz]);
         float wgt = (iz == 0 || 2 * iz == Kz) ? 1.0f : 2.0f;
@@ -765,11 +778,14 @@ __device__ __forceinline__ bool gather_vec(const float* G, const RepDev& R, cons
     return true;
 }
 
+// -q grad phi from the gradient g_d along the grid coordinates s_d = K_d (p . r_d):
+// F_j = -q sum_d g_d K_d r[j][d] (r the reciprocal box, lower triangular).
 __device__ __forceinline__ void add_grad_force(unsigned long long* F, int NA, int s, float q, float gx, float gy,
                                                float gz, const RepDev& R) {
-    fix_add(F + s, -q * gx * (float)R.K[0] * R.ibox[0]);
-    fix_add(F + NA + s, -q * gy * (float)R.K[1] * R.ibox[1]);
-    fix_add(F + 2 * (size_t)NA + s, -q * gz * (float)R.K[2] * R.ibox[2]);
+    const float g0 = gx * (float)R.K[0], g1 = gy * (float)R.K[1], g2 = gz * (float)R.K[2];
+    fix_add(F + s, -q * (g0 * R.recip[0]));
+    fix_add(F + NA + s, -q * fmaf(g1, R.recip[2], g0 * R.recip[1]));
+    fix_add(F + 2 * (size_t)NA + s, -q * fmaf(g2, R.recip[5], fmaf(g1, R.recip[4], g0 * R.recip[3])));
 }
 
 // Reciprocal-space forces of every atom that does not move (difference mode)
@@ -808,8 +824,9 @@ __device__ __noinline__ void gather_moving(const Args& a, int blk) {
         make_stencil(p.x, p.y, p.z, R, S, true);
     } else {
         const float4 d = a.displ[s];
-        make_stencil(wrapf(p.x + d.x, R.box[0], R.ibox[0]), wrapf(p.y + d.y, R.box[1], R.ibox[1]),
-                     wrapf(p.z + d.z, R.box[2], R.ibox[2]), R, S, true);
+        float x2 = p.x + d.x, y2 = p.y + d.y, z2 = p.z + d.z;
+        wrap3(x2, y2, z2, R);
+        make_stencil(x2, y2, z2, R, S, true);
     }
     float g[3], pot = 0.f;
     gather_grid(G, R, S, g, a.adjoint ? &pot : nullptr);

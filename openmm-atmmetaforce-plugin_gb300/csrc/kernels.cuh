@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace atm {
@@ -42,6 +43,15 @@ enum Res {
 };
 
 // Per-replica constants and offsets (device copy refreshed every evaluation).
+// One Stockham stage of a 1D transform of length N: radix R, Ns the product of
+// the earlier stages' radices, nb = N / R butterflies, step = N / (Ns R) (the
+// twiddle exponent's stride), mNs = ceil(2^32 / Ns) for the division by Ns.
+struct FftStage {
+    int R, Ns, nb, step;
+    unsigned mNs;
+    int pad[3];
+};
+
 struct RepDev {
     float box[4];      // L (x,y,z), unused
     float ibox[4];     // 1/L
@@ -65,11 +75,85 @@ struct RepDev {
     int conv_cta_b, conv_cta_e;
     int var_nb;               // the NonbondedForce is in the ATM variable groups
     int tw_off[3];            // FFT twiddle tables of the three grid dimensions
-    int pad0[2];
+    int fft_plan[3];          // FFT stage plans per dimension: first stage | stage count << 24
+    int pad0[1];
     double e_self;            // PME self energy (FP64, host)
     double e_disp;            // dispersion correction (FP64, host)
     double params[9];         // ATM globals
+    // Triclinic boxes, OpenMM's reduced form: a = (box[0], 0, 0),
+    // b = (tilt[0], box[1], 0), c = (tilt[1], tilt[2], box[2])
+    double tiltd[4];          // b_x, c_x, c_y (FP64), 0
+    float tilt[4];            // the same in FP32
+    float recip[8];           // reciprocal box rows r00, r10, r11, r20, r21, r22 (fractional coordinates)
+    int tric;                 // 1: some tilt is nonzero
+    float wmin;               // smallest distance between opposite faces of the box (nm)
+    int pad1[2];
 };
+
+#ifdef __CUDACC__
+// OpenMM's minimum image in a reduced box: subtract c, then b, then a, each
+// rounded to the nearest multiple (per axis when the box is orthorhombic; the
+// identity without periodic boundaries, where the inverse box is 0).
+__device__ __forceinline__ void min_image3(float& x, float& y, float& z, const RepDev& R) {
+    if (R.tric) {
+        const float kz = rintf(z * R.ibox[2]);
+        x -= kz * R.tilt[1];
+        y -= kz * R.tilt[2];
+        z -= kz * R.box[2];
+        const float ky = rintf(y * R.ibox[1]);
+        x -= ky * R.tilt[0];
+        y -= ky * R.box[1];
+        x -= R.box[0] * rintf(x * R.ibox[0]);
+    } else {
+        x -= R.box[0] * rintf(x * R.ibox[0]);
+        y -= R.box[1] * rintf(y * R.ibox[1]);
+        z -= R.box[2] * rintf(z * R.ibox[2]);
+    }
+}
+__device__ __forceinline__ void min_image3d(double& x, double& y, double& z, const RepDev& R) {
+    if (R.tric) {
+        const double kz = rint(z * R.iboxd[2]);
+        x -= kz * R.tiltd[1];
+        y -= kz * R.tiltd[2];
+        z -= kz * R.boxd[2];
+        const double ky = rint(y * R.iboxd[1]);
+        x -= ky * R.tiltd[0];
+        y -= ky * R.boxd[1];
+        x -= R.boxd[0] * rint(x * R.iboxd[0]);
+    } else {
+        x -= R.boxd[0] * rint(x * R.iboxd[0]);
+        y -= R.boxd[1] * rint(y * R.iboxd[1]);
+        z -= R.boxd[2] * rint(z * R.iboxd[2]);
+    }
+}
+// The periodic image inside the unit cell (fractional coordinates in [0, 1)).
+__device__ __forceinline__ void wrap3(float& x, float& y, float& z, const RepDev& R) {
+    const float kz = floorf(z * R.ibox[2]);
+    x -= kz * R.tilt[1];
+    y -= kz * R.tilt[2];
+    z -= kz * R.box[2];
+    const float ky = floorf(y * R.ibox[1]);
+    x -= ky * R.tilt[0];
+    y -= ky * R.box[1];
+    x -= R.box[0] * floorf(x * R.ibox[0]);
+}
+__device__ __forceinline__ void wrap3d(double& x, double& y, double& z, const RepDev& R) {
+    const double kz = floor(z * R.iboxd[2]);
+    x -= kz * R.tiltd[1];
+    y -= kz * R.tiltd[2];
+    z -= kz * R.boxd[2];
+    const double ky = floor(y * R.iboxd[1]);
+    x -= ky * R.tiltd[0];
+    y -= ky * R.boxd[1];
+    x -= R.boxd[0] * floor(x * R.iboxd[0]);
+}
+// Fractional coordinates (along a, b, c) of a position: p . column d of the reciprocal box.
+__device__ __forceinline__ void frac3(float x, float y, float z, const RepDev& R, float* f) {
+    f[0] = fmaf(z, R.recip[3], fmaf(y, R.recip[1], x * R.recip[0]));
+    f[1] = fmaf(z, R.recip[4], y * R.recip[2]);
+    f[2] = z * R.recip[5];
+}
+#endif
 
 // Parameters of one exception pair (x: chargeProd * ke, y: sigma, z: epsilon,
 // w: ke * q_i * q_j for the Ewald exclusion correction).
@@ -102,6 +186,8 @@ struct Args {
     float skin_half2;         // (skin / 2)^2
     float4* posq_ref;         // NA: positions at the last build
     const int* list_ctl;      // device control word: [0] = 1 forces a build
+    unsigned* rep_hmax;       // R: largest half-extent norm of a block (float bits; triclinic boxes)
+    int any_tric;             // 1: some replica's box is triclinic
     long long* list_counts;   // device: evaluations, list builds
     double alphad, cutoffd;
     // replicas
@@ -177,6 +263,7 @@ struct Args {
     // hand-written transforms (pme_fft.cu)
     int use_fft;              // 1: k_fft_zy / k_fft_x_conv / k_ifft_yz
     const float2* fft_tw;     // twiddles w_N^k = exp(-2 pi i k / N), per replica and dimension
+    const FftStage* fft_stages;  // stage plans (RepDev::fft_plan indexes them)
     int fft_plane_ctas;       // (grid, x-plane) CTAs of all replicas
     const int2* fft_plane;    //   (replica, grid * K0 + x)
     int fft_plane_smem;       // dynamic shared memory of a plane CTA (bytes)
@@ -202,8 +289,10 @@ void launch_fft_forward(const Args& a, cudaStream_t s);
 void launch_fft_conv(const Args& a, cudaStream_t s);
 void launch_fft_inverse(const Args& a, cudaStream_t s);
 int fft_plane_smem_bytes(int K1, int K2);
-void launch_influence(float* G, const float* moduli, const int* mod_off, const int* K, const double* box,
-                      double alpha, cudaStream_t s);
+// Stages of a 1D transform of length N appended to out; returns first | count << 24.
+int fft_plan_stages(int N, std::vector<FftStage>& out);
+void launch_influence(float* G, const float* moduli, const int* mod_off, const int* K, const double* recip,
+                      double volume, double alpha, cudaStream_t s);
 int fft_conv_smem_bytes(int K0, int nz);
 void launch_finalize(const Args& a, cudaStream_t s);
 void launch_output(const Args& a, cudaStream_t s);

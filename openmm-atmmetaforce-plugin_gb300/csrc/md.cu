@@ -42,7 +42,7 @@ struct MdDev {
     const MdConsGroup* cons;
     const MdSettle* settle;
     int n_bonds, n_angles, n_posres, n_cent, n_cons, n_settle;
-    const double* box;  // 3 per replica
+    const double* box;  // 6 per replica: ax, by, cz, bx, cx, cy (reduced box vectors)
     const int* rep_off; // R + 1
     double* ke;         // R
     int* status;
@@ -109,10 +109,19 @@ __global__ void k_md_terms(MdDev a) {
         }
     } else {
         MdPosRes p = a.posres[t - a.n_bonds - a.n_angles];
-        const double* L = a.box + 3 * p.rep;
+        const double* L = a.box + 6 * p.rep;
         double d[3] = {a.x[3 * (size_t)p.p] - p.x0, a.x[3 * (size_t)p.p + 1] - p.y0, a.x[3 * (size_t)p.p + 2] - p.z0};
-        if (p.periodic)
-            for (int k = 0; k < 3; k++) d[k] -= L[k] * rint(d[k] / L[k]);
+        if (p.periodic) {
+            // OpenMM's minimum image: c, then b, then a
+            double k = rint(d[2] / L[2]);
+            d[0] -= k * L[4];
+            d[1] -= k * L[5];
+            d[2] -= k * L[2];
+            k = rint(d[1] / L[1]);
+            d[0] -= k * L[3];
+            d[1] -= k * L[1];
+            d[0] -= L[0] * rint(d[0] / L[0]);
+        }
         double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
         if (r > p.tol) {
             double dr = r - p.tol;
@@ -541,7 +550,7 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
     std::vector<int> cent_idx;
     std::vector<double> cent_w;
     std::vector<MdConsGroup> cons;
-    std::vector<double> box(3 * (size_t)R_);
+    std::vector<double> box(6 * (size_t)R_);
     std::vector<int> rep_off(R_ + 1);
     dof_.assign(R_, 0);
     std::vector<int> bond_rep, ang_rep, pos_rep, cent_rep;
@@ -550,7 +559,10 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
         const int n = eng_->atoms(r), o = in_off_[r];
         rep_off[r] = o;
         if ((int)S.masses.size() != n) throw Error(9, "System particle count differs from the NonbondedForce's");
-        for (int k = 0; k < 3; k++) box[3 * r + k] = eng_->box(r)[k];
+        for (int k = 0; k < 3; k++) {
+            box[6 * r + k] = eng_->box(r)[k];
+            box[6 * r + 3 + k] = eng_->tilt(r)[k];
+        }
         int moving = 0;
         for (int i = 0; i < n; i++) {
             inv_m[o + i] = S.masses[i] > 0.0 ? 1.0 / S.masses[i] : 0.0;

@@ -108,7 +108,8 @@ public:
         return (int)masses.size() - 1;
     }
     std::vector<double> masses;
-    double box[3] = {2.0, 2.0, 2.0};  // OpenMM's default box
+    double box[3] = {2.0, 2.0, 2.0};  // OpenMM's default box (diagonal of the box vectors)
+    double tilt[3] = {0.0, 0.0, 0.0}; // b_x, c_x, c_y of reduced triclinic box vectors
     std::unique_ptr<NonbondedForce> nonbonded;
     std::unique_ptr<ATMMetaForce> atm;
     std::vector<Bond> bonds;

@@ -28,6 +28,7 @@
 // part is summed directly rather than as a difference of two totals.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -133,28 +134,17 @@ __device__ __forceinline__ void dft_odd(float2* v) {
     for (int k = 0; k < R; k++) v[k] = out[k];
 }
 
-// The factor of N taken by the next stage: 8, 4, 2 first, then 3, 5, 7, then
-// the smallest remaining prime.
-__device__ __forceinline__ int next_radix(int m) {
-    if ((m & 7) == 0) return 8;
-    if ((m & 3) == 0) return 4;
-    if ((m & 1) == 0) return 2;
-    if (m % 3 == 0) return 3;
-    if (m % 5 == 0) return 5;
-    if (m % 7 == 0) return 7;
-    for (int p = 11; p * p <= m; p += 2)
-        if (m % p == 0) return p;
-    return m;
-}
-
 // Division by a divisor 1 <= d < 2^16 fixed for a loop, for non-negative
-// w < 2^23: q = umulhi(w, m) with m ~ 2^32 / d from an FP32 division (within
-// 2^8 of the exact value, so q is off by at most one), then corrected.  Four
-// integer instructions per division instead of a runtime division's sequence.
+// w < 2^23: q = umulhi(w, m) with m >= 2^32 / d close to it, so that q is
+// floor(w / d) or one more, then corrected.  m is either exact (ceil(2^32 / d),
+// from the host's stage plans) or from an FP32 division (within 2^8 of it, q
+// then off by at most one either way).  Four integer instructions per division
+// instead of a runtime division's sequence.
 struct FastDiv {
     unsigned d, m;
     __device__ __forceinline__ explicit FastDiv(int dd)
         : d((unsigned)dd), m(dd > 1 ? (unsigned)(4294967296.0f / (float)dd) : 0u) {}
+    __device__ __forceinline__ FastDiv(unsigned dd, unsigned mm) : d(dd), m(mm) {}
     __device__ __forceinline__ unsigned div(unsigned w) const {
         if (d == 1) return w;
         unsigned q = __umulhi(w, m);
@@ -163,24 +153,21 @@ struct FastDiv {
     }
 };
 
-// One Stockham stage of radix R (specialised) over nseq sequences of length N:
-// element e of sequence q at q * ss + e * es.  Butterfly j (0 <= j < N/R) reads
-// x[j + r N/R], twiddles it by w_N^{r k N/(Ns R)} (k = j mod Ns) and writes its R
-// outputs to (j / Ns) Ns R + k + r Ns.  Work items run sequence-fastest when the
-// elements of a sequence are strided (column transforms), element-fastest when
-// they are contiguous, so that neighbouring threads touch neighbouring words.
+// One Stockham stage of radix R (specialised) over nseq sequences of length N
+// (element e of sequence q at q * ss + e * es), as planned on the host: Ns the
+// product of the earlier radices, nb = N / R butterflies, step = N / (Ns R).
+// Butterfly j reads x[j + r nb], twiddles it by w_N^{r k step} (k = j mod Ns) and
+// writes its R outputs to (j / Ns) Ns R + k + r Ns.  Work items run
+// sequence-fastest: neighbouring threads take neighbouring sequences, whose
+// starts the callers space by an odd number of words' pairs (no bank conflicts).
 template <int R, bool INV>
-__device__ __forceinline__ void stage_r(const float2* src, float2* dst, int N, int Ns, int nseq, int ss, int es,
-                                        const float2* tw) {
-    const int nb = N / R;
-    const int items = nb * nseq;
-    const int step = N / (Ns * R);
-    const bool seq_fast = es != 1;
-    const FastDiv fd(seq_fast ? nseq : nb), fns(Ns);
+__device__ __forceinline__ void stage_r(const float2* src, float2* dst, const FftStage& p, const FastDiv& fq,
+                                        int ss, int es, const float2* tw) {
+    const int nb = p.nb, Ns = p.Ns, step = p.step;
+    const int items = nb * (int)fq.d;
+    const FastDiv fns((unsigned)Ns, p.mNs);
     for (int w = threadIdx.x; w < items; w += blockDim.x) {
-        const int a = (int)fd.div((unsigned)w), b = w - a * fd.d;  // w = a d + b
-        const int q = seq_fast ? b : a;
-        const int j = seq_fast ? a : b;
+        const int j = (int)fq.div((unsigned)w), q = w - j * (int)fq.d;
         const int jn = (int)fns.div((unsigned)j);
         const int k = j - jn * Ns;
         const float2* s = src + q * ss;
@@ -204,15 +191,12 @@ __device__ __forceinline__ void stage_r(const float2* src, float2* dst, int N, i
 // Direct DFT stage for a prime factor R outside the dedicated radices: one work
 // item per output (sum over the R twiddled inputs).
 template <bool INV>
-__device__ __forceinline__ void stage_generic(const float2* src, float2* dst, int N, int R, int Ns, int nseq, int ss,
-                                              int es, const float2* tw) {
-    const int nb = N / R;
-    const int items = N * nseq;
-    const int step = N / (Ns * R);
-    const bool seq_fast = es != 1;
+__device__ __forceinline__ void stage_generic(const float2* src, float2* dst, const FftStage& p, int N,
+                                              const FastDiv& fq, int ss, int es, const float2* tw) {
+    const int R = p.R, nb = p.nb, Ns = p.Ns, step = p.step;
+    const int items = N * (int)fq.d;
     for (int w = threadIdx.x; w < items; w += blockDim.x) {
-        const int q = seq_fast ? w % nseq : w / N;
-        const int t = seq_fast ? w / nseq : w % N;  // (butterfly j, output m)
+        const int t = (int)fq.div((unsigned)w), q = w - t * (int)fq.d;  // t: (butterfly j, output m)
         const int j = t % nb, m = t / nb;
         const int k = j % Ns;
         const float2* s = src + q * ss;
@@ -227,32 +211,38 @@ __device__ __forceinline__ void stage_generic(const float2* src, float2* dst, in
     }
 }
 
-// nseq transforms of length N between buf[0] and buf[1] (same layout); returns
-// the index of the buffer holding the result.  Every thread of the CTA calls it.
+// nseq transforms of length N between buf0 and buf1 (same layout) following the
+// host's plan (plan: first stage | count << 24); returns 1 when the result is in
+// buf1, 0 when in buf0.  Every thread of the CTA calls it.
 template <bool INV>
-__device__ int fft_seqs(float2* buf0, float2* buf1, int N, int nseq, int ss, int es, const float2* tw) {
+__device__ int fft_seqs(const Args& a, int plan, float2* buf0, float2* buf1, int N, int nseq, int ss, int es,
+                        const float2* tw) {
+    const FftStage* st = a.fft_stages + (plan & 0xffffff);
+    const int nst = plan >> 24;
+    const FastDiv fq(nseq);
     int cur = 0;
-    int Ns = 1, m = N;
-    while (m > 1) {
-        const int R = next_radix(m);
+    for (int k = 0; k < nst; k++) {
+        const FftStage p = st[k];
         const float2* src = cur ? buf1 : buf0;
         float2* dst = cur ? buf0 : buf1;
-        switch (R) {
-            case 8: stage_r<8, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            case 4: stage_r<4, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            case 2: stage_r<2, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            case 3: stage_r<3, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            case 5: stage_r<5, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            case 7: stage_r<7, INV>(src, dst, N, Ns, nseq, ss, es, tw); break;
-            default: stage_generic<INV>(src, dst, N, R, Ns, nseq, ss, es, tw); break;
+        switch (p.R) {
+            case 8: stage_r<8, INV>(src, dst, p, fq, ss, es, tw); break;
+            case 4: stage_r<4, INV>(src, dst, p, fq, ss, es, tw); break;
+            case 2: stage_r<2, INV>(src, dst, p, fq, ss, es, tw); break;
+            case 3: stage_r<3, INV>(src, dst, p, fq, ss, es, tw); break;
+            case 5: stage_r<5, INV>(src, dst, p, fq, ss, es, tw); break;
+            case 7: stage_r<7, INV>(src, dst, p, fq, ss, es, tw); break;
+            default: stage_generic<INV>(src, dst, p, N, fq, ss, es, tw); break;
         }
         __syncthreads();
         cur ^= 1;
-        Ns *= R;
-        m /= R;
     }
     return cur;
 }
+
+// Row stride of the z transforms: odd, so that sequence-fastest accesses to
+// neighbouring rows fall in different banks.
+__device__ __forceinline__ int zrow(int K2) { return K2 | 1; }
 
 // Twiddle tables of the three grid dimensions of a replica, copied to shared memory.
 __device__ __forceinline__ void load_tw(const Args& a, const RepDev& R, int d, float2* out) {
@@ -270,7 +260,8 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
     const RepDev& R = a.reps[pc.x];
     const int K0 = R.K[0], K1 = R.K[1], K2 = R.K[2], K2h = K2 / 2 + 1, P = (K1 + 1) / 2;
     const int g = pc.y / K0, ix = pc.y - g * K0;
-    const int plane = max(P * K2, K1 * K2h);
+    const int zs = zrow(K2);
+    const int plane = max(P * zs, K1 * K2h);
     float2* b0 = sh;
     float2* b1 = sh + plane;
     float2* tw1 = sh + 2 * plane;
@@ -288,7 +279,7 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
             const int p = (int)f4.div((unsigned)w), z4 = w - p * q4;
             const float4 re = G4[(2 * p) * q4 + z4];
             const float4 im = 2 * p + 1 < K1 ? G4[(2 * p + 1) * q4 + z4] : make_float4(0.f, 0.f, 0.f, 0.f);
-            float2* d = b0 + p * K2 + 4 * z4;
+            float2* d = b0 + p * zs + 4 * z4;
             d[0] = make_float2(re.x, im.x);
             d[1] = make_float2(re.y, im.y);
             d[2] = make_float2(re.z, im.z);
@@ -300,11 +291,11 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
             const int p = (int)fz.div((unsigned)w), z = w - p * K2;
             const float re = G[(size_t)(2 * p) * K2 + z];
             const float im = 2 * p + 1 < K1 ? G[(size_t)(2 * p + 1) * K2 + z] : 0.f;
-            b0[w] = make_float2(re, im);
+            b0[p * zs + z] = make_float2(re, im);
         }
     }
     __syncthreads();
-    const int cz = fft_seqs<false>(b0, b1, K2, P, K2, 1, tw2);
+    const int cz = fft_seqs<false>(a, R.fft_plan[2], b0, b1, K2, P, zs, 1, tw2);
     const float2* Z = cz ? b1 : b0;
     float2* S = cz ? b0 : b1;
     // Z = A + iB of two real rows: A_k = (Z_k + conj Z_-k) / 2, B_k = (Z_k - conj Z_-k) / (2i)
@@ -312,13 +303,13 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
     for (int w = threadIdx.x; w < K1 * K2h; w += blockDim.x) {
         const int y = (int)fh.div((unsigned)w), kz = w - y * K2h;
         const int p = y >> 1;
-        const float2 zp = Z[p * K2 + kz], zm = Z[p * K2 + (kz == 0 ? 0 : K2 - kz)];
+        const float2 zp = Z[p * zs + kz], zm = Z[p * zs + (kz == 0 ? 0 : K2 - kz)];
         S[w] = (y & 1) ? make_float2(0.5f * (zp.y + zm.y), 0.5f * (zm.x - zp.x))
                        : make_float2(0.5f * (zp.x + zm.x), 0.5f * (zp.y - zm.y));
     }
     __syncthreads();
     float2* Zw = const_cast<float2*>(Z);
-    const int cy = fft_seqs<false>(S, Zw, K1, K2h, 1, K2h, tw1);
+    const int cy = fft_seqs<false>(a, R.fft_plan[1], S, Zw, K1, K2h, 1, K2h, tw1);
     const float2* Y = cy ? Zw : S;
     float2* out = a.qcplx + R.cplx_off + (size_t)g * K0 * K1 * K2h + (size_t)ix * K2h;
 #pragma unroll 4
@@ -334,7 +325,8 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
     const RepDev& R = a.reps[pc.x];
     const int K0 = R.K[0], K1 = R.K[1], K2 = R.K[2], K2h = K2 / 2 + 1, P = (K1 + 1) / 2;
     const int g = pc.y / K0, ix = pc.y - g * K0;
-    const int plane = max(P * K2, K1 * K2h);
+    const int zs = zrow(K2);
+    const int plane = max(P * zs, K1 * K2h);
     float2* b0 = sh;
     float2* b1 = sh + plane;
     float2* tw1 = sh + 2 * plane;
@@ -349,7 +341,7 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
         b0[w] = in[(size_t)y * K0 * K2h + kz];
     }
     __syncthreads();
-    const int cy = fft_seqs<true>(b0, b1, K1, K2h, 1, K2h, tw1);
+    const int cy = fft_seqs<true>(a, R.fft_plan[1], b0, b1, K1, K2h, 1, K2h, tw1);
     const float2* S = cy ? b1 : b0;
     float2* Z = cy ? b0 : b1;
     // two rows' Hermitian half spectra as one complex row Z = A + iB (the
@@ -368,11 +360,11 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
             A.y = -A.y;
             B.y = -B.y;
         }
-        Z[w] = make_float2(A.x - B.y, A.y + B.x);
+        Z[p * zs + z] = make_float2(A.x - B.y, A.y + B.x);
     }
     __syncthreads();
     float2* Sw = const_cast<float2*>(S);
-    const int cz = fft_seqs<true>(Z, Sw, K2, P, K2, 1, tw2);
+    const int cz = fft_seqs<true>(a, R.fft_plan[2], Z, Sw, K2, P, zs, 1, tw2);
     const float2* Zr = cz ? Sw : Z;
     float* G = a.qreal + R.real_off + (size_t)g * K0 * K1 * K2 + (size_t)ix * K1 * K2;
     if ((K2 & 3) == 0) {
@@ -381,14 +373,14 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
         float4* G4 = reinterpret_cast<float4*>(G);
         for (int w = threadIdx.x; w < K1 * q4; w += blockDim.x) {
             const int y = (int)f4.div((unsigned)w), z4 = w - y * q4;
-            const float2* zr = Zr + (y >> 1) * K2 + 4 * z4;
+            const float2* zr = Zr + (y >> 1) * zs + 4 * z4;
             const float2 v0 = zr[0], v1 = zr[1], v2 = zr[2], v3 = zr[3];
             G4[w] = (y & 1) ? make_float4(v0.y, v1.y, v2.y, v3.y) : make_float4(v0.x, v1.x, v2.x, v3.x);
         }
     } else {
         for (int w = threadIdx.x; w < K1 * K2; w += blockDim.x) {
             const int y = (int)fz.div((unsigned)w), z = w - y * K2;
-            const float2 v = Zr[(y >> 1) * K2 + z];
+            const float2 v = Zr[(y >> 1) * zs + z];
             G[w] = (y & 1) ? v.y : v.x;
         }
     }
@@ -417,7 +409,7 @@ __global__ void __launch_bounds__(kFftThreads, 4) k_fft_x_conv(Args a) {
         b0[w] = slab[g * C3 + (size_t)x * K2h + kz];
     }
     __syncthreads();
-    int cur = fft_seqs<false>(b0, b1, K0, W, 1, W, tw0);
+    int cur = fft_seqs<false>(a, R.fft_plan[0], b0, b1, K0, W, 1, W, tw0);
     float2* M = cur ? b1 : b0;
     // influence function G(m) = exp(-pi^2 m^2 / alpha^2) / (pi V m^2 B(m)), B the
     // B-spline moduli; the half spectrum counts kz in (0, K2/2) twice
@@ -452,7 +444,7 @@ __global__ void __launch_bounds__(kFftThreads, 4) k_fft_x_conv(Args a) {
         a.e_part_conv[2 * blockIdx.x + threadIdx.x] = t;
     }
     float2* other = cur ? b0 : b1;
-    cur = fft_seqs<true>(M, other, K0, W, 1, W, tw0);
+    cur = fft_seqs<true>(a, R.fft_plan[0], M, other, K0, W, 1, W, tw0);
     const float2* out = cur ? other : M;
 #pragma unroll 4
     for (int w = threadIdx.x; w < K0 * W; w += blockDim.x) {
@@ -468,7 +460,8 @@ __global__ void __launch_bounds__(kFftThreads, 4) k_fft_x_conv(Args a) {
 // al. 1995).  It depends only on the box, the grid and alpha, so it is computed
 // when buffers are made or a box changes, not at every evaluation.
 __global__ void k_influence(float* G, const float* mx, const float* my, const float* mz, int K0, int K1, int K2,
-                            double Lx, double Ly, double Lz, double alpha) {
+                            double r00, double r10, double r11, double r20, double r21, double r22, double vol,
+                            double alpha) {
     const int K2h = K2 / 2 + 1;
     const long long n = (long long)K0 * K1 * K2h;
     const double pi = 3.14159265358979323846;
@@ -477,29 +470,55 @@ __global__ void k_influence(float* G, const float* mx, const float* my, const fl
         const long long r = e / K2h;
         const int x = (int)(r % K0), ky = (int)(r / K0);
         const int mxi = x <= K0 / 2 ? x : x - K0, myi = ky <= K1 / 2 ? ky : ky - K1;
-        const double kx = mxi / Lx, kyv = myi / Ly, kzv = kz / Lz;
+        // m = mx a* + my b* + mz c*, the reciprocal vectors being the columns of r
+        const double kx = mxi * r00, kyv = mxi * r10 + myi * r11, kzv = mxi * r20 + myi * r21 + kz * r22;
         const double m2 = kx * kx + kyv * kyv + kzv * kzv;
         double g = 0.0;
         if (e != 0 || m2 > 0.0)
             g = m2 > 0.0 ? exp(-pi * pi * m2 / (alpha * alpha)) /
-                               (pi * Lx * Ly * Lz * m2 * (double)mx[x] * (double)my[ky] * (double)mz[kz])
+                               (pi * vol * m2 * (double)mx[x] * (double)my[ky] * (double)mz[kz])
                          : 0.0;
         G[e] = (float)g;
     }
 }
 
-void launch_influence(float* G, const float* moduli, const int* mod_off, const int* K, const double* box,
-                      double alpha, cudaStream_t s) {
+void launch_influence(float* G, const float* moduli, const int* mod_off, const int* K, const double* recip,
+                      double volume, double alpha, cudaStream_t s) {
     const long long n = (long long)K[0] * K[1] * (K[2] / 2 + 1);
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
     k_influence<<<blocks, 256, 0, s>>>(G, moduli + mod_off[0], moduli + mod_off[1], moduli + mod_off[2], K[0], K[1],
-                                      K[2], box[0], box[1], box[2], alpha);
+                                      K[2], recip[0], recip[1], recip[2], recip[3], recip[4], recip[5], volume, alpha);
 }
 
 int fft_plane_smem_bytes(int K1, int K2) {
-    const int P = (K1 + 1) / 2, K2h = K2 / 2 + 1;
-    const int plane = P * K2 > K1 * K2h ? P * K2 : K1 * K2h;
+    const int P = (K1 + 1) / 2, K2h = K2 / 2 + 1, zs = K2 | 1;
+    const int plane = P * zs > K1 * K2h ? P * zs : K1 * K2h;
     return (int)sizeof(float2) * (2 * plane + K1 + K2);
+}
+
+// Radices 8 (as many as divide N), then 4 or 2 for the rest of the power of two,
+// then 3, 5, 7 and any other prime factor, smallest first.
+int fft_plan_stages(int N, std::vector<FftStage>& out) {
+    std::vector<int> rad;
+    int n = N;
+    while (n % 8 == 0) { rad.push_back(8); n /= 8; }
+    if (n % 4 == 0) { rad.push_back(4); n /= 4; }
+    if (n % 2 == 0) { rad.push_back(2); n /= 2; }
+    for (int p = 3; n > 1; p += 2)
+        while (n % p == 0) { rad.push_back(p); n /= p; }
+    const int first = (int)out.size();
+    int Ns = 1;
+    for (int R : rad) {
+        FftStage st{};
+        st.R = R;
+        st.Ns = Ns;
+        st.nb = N / R;
+        st.step = N / (Ns * R);
+        st.mNs = Ns > 1 ? (unsigned)((0x100000000ull + (unsigned long long)Ns - 1) / (unsigned long long)Ns) : 0u;
+        out.push_back(st);
+        Ns *= R;
+    }
+    return first | (int)rad.size() << 24;
 }
 
 int fft_conv_smem_bytes(int K0, int nz) { return (int)sizeof(float2) * (2 * K0 * 2 * nz + K0); }

@@ -41,20 +41,83 @@ __device__ __forceinline__ void fix_add_t(unsigned long long* p, float v) {
     atomicAdd(p, fix_bits(v));
 }
 
-__device__ __forceinline__ float min_img(float d, float L, float iL) { return d - L * rintf(d * iL); }
-
-__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj, const RepDev& R, float rc2) {
-    float dx = fmaxf(0.f, fabsf(min_img(cj.x - ci.x, R.box[0], R.ibox[0])) - hi.x - hj.x);
-    float dy = fmaxf(0.f, fabsf(min_img(cj.y - ci.y, R.box[1], R.ibox[1])) - hi.y - hj.y);
-    float dz = fmaxf(0.f, fabsf(min_img(cj.z - ci.z, R.box[2], R.ibox[2])) - hi.z - hj.z);
-    return dx * dx + dy * dy + dz * dz < rc2;
+// The box of a replica in registers, for minimum images in the pair loops.
+struct ImgBox {
+    float Lx, Ly, Lz, iLx, iLy, iLz, bx, cx, cy;
+    int tric;
+};
+__device__ __forceinline__ ImgBox img_box(const RepDev& R) {
+    return ImgBox{R.box[0], R.box[1], R.box[2], R.ibox[0], R.ibox[1], R.ibox[2], R.tilt[0], R.tilt[1], R.tilt[2],
+                  R.tric};
+}
+// OpenMM's minimum image (reduced triclinic box: c, then b, then a; per axis
+// when orthorhombic)
+__device__ __forceinline__ void min_image_b(float& x, float& y, float& z, const ImgBox& B) {
+    if (B.tric) {
+        const float kz = rintf(z * B.iLz);
+        x -= kz * B.cx;
+        y -= kz * B.cy;
+        z -= kz * B.Lz;
+        const float ky = rintf(y * B.iLy);
+        x -= ky * B.bx;
+        y -= ky * B.Ly;
+    } else {
+        y -= B.Ly * rintf(y * B.iLy);
+        z -= B.Lz * rintf(z * B.iLz);
+    }
+    x -= B.Lx * rintf(x * B.iLx);
 }
 
+// The finder's minimum image: its orthorhombic instantiation (no replica of the
+// batch is triclinic) keeps only the per-axis form, and none of the tilts.
+// (The box is read from the replica's table where it is used: held in registers
+// across a row it costs the finder spills.)
+template <bool TRIC>
+__device__ __forceinline__ void min_image_t(float& x, float& y, float& z, const RepDev& R) {
+    if constexpr (TRIC) {
+        min_image3(x, y, z, R);
+    } else {
+        x -= R.box[0] * rintf(x * R.ibox[0]);
+        y -= R.box[1] * rintf(y * R.ibox[1]);
+        z -= R.box[2] * rintf(z * R.ibox[2]);
+    }
+}
+
+__device__ __forceinline__ float box_gap2(float dx, float dy, float dz, float hx, float hy, float hz) {
+    dx = fmaxf(0.f, fabsf(dx) - hx);
+    dy = fmaxf(0.f, fabsf(dy) - hy);
+    dz = fmaxf(0.f, fabsf(dz) - hz);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Are two blocks' bounding boxes closer than the cutoff?  The centres' minimum
+// image (per axis, exact for orthorhombic boxes); triclinic rows that need
+// per-pair images (all_images) take the closest of the 125 images around it.
+template <bool TRIC>
+__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj, const RepDev& R, float rc2,
+                                            bool all_images = false) {
+    float dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
+    min_image_t<TRIC>(dx, dy, dz, R);
+    const float hx = hi.x + hj.x, hy = hi.y + hj.y, hz = hi.z + hj.z;
+    if (!TRIC || !all_images) return box_gap2(dx, dy, dz, hx, hy, hz) < rc2;
+    for (int k = -2; k <= 2; k++)
+        for (int j = -2; j <= 2; j++)
+            for (int i = -2; i <= 2; i++) {
+                const float vx = dx + i * R.box[0] + j * R.tilt[0] + k * R.tilt[1];
+                const float vy = dy + j * R.box[1] + k * R.tilt[2];
+                const float vz = dz + k * R.box[2];
+                if (box_gap2(vx, vy, vz, hx, hy, hz) < rc2) return true;
+            }
+    return false;
+}
+
+// Is atom p within the cutoff of the box of block I (minimum image of the offset
+// from the box centre)?
+template <bool TRIC>
 __device__ __forceinline__ bool point_close(float4 ci, float4 hi, float4 p, const RepDev& R, float rc2) {
-    float dx = fmaxf(0.f, fabsf(min_img(p.x - ci.x, R.box[0], R.ibox[0])) - hi.x);
-    float dy = fmaxf(0.f, fabsf(min_img(p.y - ci.y, R.box[1], R.ibox[1])) - hi.y);
-    float dz = fmaxf(0.f, fabsf(min_img(p.z - ci.z, R.box[2], R.ibox[2])) - hi.z);
-    return dx * dx + dy * dy + dz * dz < rc2;
+    float dx = p.x - ci.x, dy = p.y - ci.y, dz = p.z - ci.z;
+    min_image_t<TRIC>(dx, dy, dz, R);
+    return box_gap2(dx, dy, dz, hi.x, hi.y, hi.z) < rc2;
 }
 
 // Centre and half extent of block I at the geometry of a row.
@@ -93,12 +156,12 @@ __device__ __forceinline__ float4 row_pos(const Args& a, int kind, int s) {
 // warp's shared memory for the exact cut: FP32 (absolute), or with hcut the
 // offsets from the box centre as half2 pairs (atoms 2m, 2m+1: x, y, z; 16 bytes
 // per pair, in the first half of the same buffer).
+template <bool TRIC>
 __device__ __forceinline__ void load_ipos(const Args& a, const RepDev& R, int I, int kind, float4 ci, int lane,
                                           float4* s_ipos, bool hcut) {
     const float4 pi = row_pos(a, kind, I * kTile + lane);
-    const float rx = min_img(pi.x - ci.x, R.box[0], R.ibox[0]);
-    const float ry = min_img(pi.y - ci.y, R.box[1], R.ibox[1]);
-    const float rz = min_img(pi.z - ci.z, R.box[2], R.ibox[2]);
+    float rx = pi.x - ci.x, ry = pi.y - ci.y, rz = pi.z - ci.z;
+    min_image_t<TRIC>(rx, ry, rz, R);
     if (hcut) {
         const float nx = __shfl_down_sync(FULL_MASK, rx, 1), ny = __shfl_down_sync(FULL_MASK, ry, 1),
                     nz = __shfl_down_sync(FULL_MASK, rz, 1);
@@ -136,6 +199,7 @@ constexpr float kHalfCutMaxH = 0.75f, kHalfCutMaxRc = 1.5f, kHalfCutMargin = 0.0
 // returns from + the number kept.
 constexpr unsigned kHalfA = 1u << 30, kHalfB = 1u << 31, kSlotBits = kHalfA - 1u;
 
+template <bool TRIC>
 __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, int kind, float4 ci, int lane,
                                               int* list, int from, int natom, const float4* s_ipos) {
     const float rcm = sqrtf(a.rcl2) + kHalfCutMargin;
@@ -149,9 +213,10 @@ __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, in
         float rx = 64.f, ry = 64.f, rz = 64.f;  // invalid lanes never hit
         if (valid) {
             const float4 p = row_pos(a, kind, j);
-            rx = min_img(p.x - ci.x, R.box[0], R.ibox[0]);
-            ry = min_img(p.y - ci.y, R.box[1], R.ibox[1]);
-            rz = min_img(p.z - ci.z, R.box[2], R.ibox[2]);
+            rx = p.x - ci.x;
+            ry = p.y - ci.y;
+            rz = p.z - ci.z;
+            min_image_t<TRIC>(rx, ry, rz, R);
         }
         const __half2 hx = __float2half2_rn(rx), hy = __float2half2_rn(ry), hz = __float2half2_rn(rz);
         bool hitA = false, hitB = false;
@@ -192,9 +257,10 @@ __device__ __forceinline__ int exact_cut_half(const Args& a, const RepDev& R, in
     return kept;
 }
 
+template <bool TRIC>
 __device__ __noinline__ int exact_cut(const Args& a, const RepDev& R, int kind, float4 ci, int lane, int* list,
                                          int from, int natom, const float4* s_ipos, bool hcut) {
-    if (hcut) return exact_cut_half(a, R, kind, ci, lane, list, from, natom, s_ipos);
+    if (hcut) return exact_cut_half<TRIC>(a, R, kind, ci, lane, list, from, natom, s_ipos);
     const float rc2 = a.rcl2 * 1.00001f;
     int kept = from;
     for (int g = from; g < natom; g += 32) {
@@ -205,9 +271,11 @@ __device__ __noinline__ int exact_cut(const Args& a, const RepDev& R, int kind, 
         float4 p = make_float4(1.0e15f, 1.0e15f, 1.0e15f, 0.f);  // invalid lanes never hit
         if (valid) {
             p = row_pos(a, kind, j);
-            p.x = ci.x + min_img(p.x - ci.x, R.box[0], R.ibox[0]);
-            p.y = ci.y + min_img(p.y - ci.y, R.box[1], R.ibox[1]);
-            p.z = ci.z + min_img(p.z - ci.z, R.box[2], R.ibox[2]);
+            float rx = p.x - ci.x, ry = p.y - ci.y, rz = p.z - ci.z;
+            min_image_t<TRIC>(rx, ry, rz, R);
+            p.x = ci.x + rx;
+            p.y = ci.y + ry;
+            p.z = ci.z + rz;
         }
         // eight i atoms at a time; each half until every lane has decided it
         for (int q0 = 0; q0 < kHalf; q0 += 8) {
@@ -251,11 +319,11 @@ __device__ __noinline__ int exact_cut(const Args& a, const RepDev& R, int kind, 
 // The row's exclusion partners are held one per lane (rows with more than 32 fall
 // back to reading the list), and four candidate blocks are loaded per step so
 // that their latencies overlap.
-template <bool CUT>
+template <bool CUT, bool TRIC>
 __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, int kind, float4 ci, float4 hi,
                                          const int2* ee, int e0, int e1, int lane, int* out, int cap,
                                          const float4* s_ipos, int& raw, int first, int stride,
-                                         bool hcut = false) {
+                                         bool hcut = false, bool all_images = false) {
     const bool diff = kind >= ROW_DIFF1;
     const bool g2 = kind == ROW_DIFF2;
     const int cls_i = a.block_cls[I];
@@ -289,7 +357,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
                     cj4.z += dd.z;
                 }
             }
-            ok = boxes_close(ci, hi, cj4, hj4, R, a.rcl2);
+            ok = boxes_close<TRIC>(ci, hi, cj4, hj4, R, a.rcl2, all_images);
             if (nex > 32)
                 for (int k = e0; ok && k < e1; k++)
                     if (ee[k].x == Jl) ok = false;
@@ -327,7 +395,8 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             }
 #pragma unroll
             for (int t = 0; t < 4; t++) {
-                const bool in = lane < n[t] && point_close(ci, hi, p[t], R, a.rcl2);
+                // (triclinic rows with per-pair images keep every atom of a candidate block)
+                const bool in = lane < n[t] && (all_images || point_close<TRIC>(ci, hi, p[t], R, a.rcl2));
                 const unsigned b = __ballot_sync(FULL_MASK, in);
                 const int k = natom + __popc(b & ((1u << lane) - 1u));
                 if (in && k < cap && !over) out[k] = J[t] * kTile + lane;
@@ -336,7 +405,7 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
             }
             if (CUT && !over && natom > cap - 4 * kTile) {
                 __syncwarp();
-                natom = exact_cut(a, R, kind, ci, lane, out, cut_from, min(natom, cap), s_ipos, hcut);
+                natom = exact_cut<TRIC>(a, R, kind, ci, lane, out, cut_from, min(natom, cap), s_ipos, hcut);
                 cut_from = natom;
                 over = natom > cap - 4 * kTile;
             }
@@ -345,12 +414,13 @@ __device__ __forceinline__ int row_atoms(const Args& a, const RepDev& R, int I, 
     if (CUT) {
         if (over) return -1;
         __syncwarp();
-        natom = exact_cut(a, R, kind, ci, lane, out, cut_from, natom, s_ipos, hcut);
+        natom = exact_cut<TRIC>(a, R, kind, ci, lane, out, cut_from, natom, s_ipos, hcut);
     }
     return natom;
 }
 
 // The tiles of one row (one warp; stage and ipos: the warp's shared memory).
+template <bool TRIC>
 __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* stage, float4* ipos) {
     const int4 d = a.row_desc[row];
     const int I = d.x, kind = d.y;
@@ -368,21 +438,31 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     // cutoff sphere around block I reaches half a box length (at the list cutoff:
     // while the lists are kept, a block's box grows by up to skin / 2 per side)
     const float rc = sqrtf(a.rcl2);
-    const unsigned pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
-                          rc + 2.f * hi.z >= 0.5f * R.box[2])
-                             ? 1u
-                             : 0u;
+    unsigned pbc;
+    if (TRIC && R.tric) {
+        // images are coupled across axes: the centres' minimum image is the one of
+        // every pair when rc plus both blocks' half extents (the replica's largest
+        // for J) stays below half the smallest face distance
+        const float hn = sqrtf(hi.x * hi.x + hi.y * hi.y + hi.z * hi.z);
+        pbc = rc + hn + __uint_as_float(a.rep_hmax[d.z]) >= 0.5f * R.wmin ? 1u : 0u;
+    } else {
+        pbc = (rc + 2.f * hi.x >= 0.5f * R.box[0] || rc + 2.f * hi.y >= 0.5f * R.box[1] ||
+               rc + 2.f * hi.z >= 0.5f * R.box[2])
+                  ? 1u
+                  : 0u;
+    }
+    const bool all_images = TRIC && pbc && R.tric;
     // staged in shared memory and cut there; rows whose atoms do not fit, and rows
     // that need per-pair images (no exact cut), are written by a second pass
     int raw = 0, natom = -1;
     if (!pbc) {
         const bool hcut = rc <= kHalfCutMaxRc && fmaxf(hi.x, fmaxf(hi.y, hi.z)) <= kHalfCutMaxH;
-        load_ipos(a, R, I, kind, ci, lane, ipos, hcut);
-        natom = row_atoms<true>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
+        load_ipos<TRIC>(a, R, I, kind, ci, lane, ipos, hcut);
+        natom = row_atoms<true, TRIC>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
                                 nparts, hcut);
     } else {
-        natom = row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
-                                 nparts);
+        natom = row_atoms<false, TRIC>(a, R, I, kind, ci, hi, ee, e0, e1, lane, stage, kStageAtoms, ipos, raw, part,
+                                 nparts, false, all_images);
         if (natom > kStageAtoms) natom = -1;
     }
     __syncwarp();
@@ -449,8 +529,10 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
         }
     } else {
         // second pass: the same atoms, in the same order, straight into the j slots of both halves
-        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outA, natom, ipos, raw, part, nparts);
-        row_atoms<false>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outB, natom, ipos, raw, part, nparts);
+        row_atoms<false, TRIC>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outA, natom, ipos, raw, part, nparts, false,
+                         all_images);
+        row_atoms<false, TRIC>(a, R, I, kind, ci, hi, ee, e0, e1, lane, outB, natom, ipos, raw, part, nparts, false,
+                         all_images);
     }
     for (int k = nA + lane; k < kHalf * nta; k += 32) outA[k] = -1;
     for (int k = nB + lane; k < kHalf * ntb; k += 32) outB[k] = -1;
@@ -474,6 +556,7 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
 // state-2 / difference rows at the end of the row list scan every block of
 // their replica and are the longest, so they start early); the next row is
 // requested before the current one is built.
+template <bool TRIC>
 __global__ void __launch_bounds__(kFindWarps * 32, 6) k_find(Args a) {
     __shared__ int s_stage[kFindWarps][kStageAtoms];
     __shared__ float4 s_ipos[kFindWarps][32];
@@ -488,7 +571,7 @@ __global__ void __launch_bounds__(kFindWarps * 32, 6) k_find(Args a) {
     int mine = a.nrows;
     while (k < a.nrows) {
         if (lane == 0) mine = nw < a.nrows ? nw + atomicAdd(&a.status->next_row, 1) : a.nrows;
-        find_row(a, a.nrows - 1 - k, lane, s_stage[w], s_ipos[w]);
+        find_row<TRIC>(a, a.nrows - 1 - k, lane, s_stage[w], s_ipos[w]);
         __syncwarp();
         k = __shfl_sync(FULL_MASK, mine, 0);
     }
@@ -496,7 +579,7 @@ __global__ void __launch_bounds__(kFindWarps * 32, 6) k_find(Args a) {
 
 int find_warps_per_sm() {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, kFindWarps * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find<true>, kFindWarps * 32, 0);
     return std::max(1, per_sm) * kFindWarps;
 }
 
@@ -506,11 +589,14 @@ void launch_find(const Args& a, cudaStream_t s) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find, kFindWarps * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_find<true>, kFindWarps * 32, 0);
         if (per_sm < 1) per_sm = 1;
     }
     const int blocks = std::min(per_sm * sms, (a.nrows + kFindWarps - 1) / kFindWarps);
-    k_find<<<blocks, kFindWarps * 32, 0, s>>>(a);
+    if (a.any_tric)
+        k_find<true><<<blocks, kFindWarps * 32, 0, s>>>(a);
+    else
+        k_find<false><<<blocks, kFindWarps * 32, 0, s>>>(a);
 }
 
 // The hardware approximations of the PTX ISA with subnormal inputs and results
@@ -578,9 +664,9 @@ __device__ __forceinline__ void pair_eval(float r2, float qq, float sig, float e
 // count (exclusions, padding); unmasked tiles park their padding j slots far away.
 template <int METHOD, bool PBC, bool DIFF, bool MASKED>
 __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
-                                           float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
-                                           float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
-                                           float crf, float3& fi, float3& fj, float& e32, double& e64) {
+                                           float2 li, unsigned mask, int lane, const ImgBox& B, float rc2,
+                                           float alpha, float krf, float crf, float3& fi, float3& fj, float& e32,
+                                           double& e64) {
     const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     // the unmasked atom tiles carry most pairs; the other variants stay compact
     // so that the hot loop keeps the instruction cache
@@ -590,11 +676,7 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
         const float4 pj = sp[k];
         const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-        if (PBC) {
-            dx = min_img(dx, Lx, iLx);
-            dy = min_img(dy, Ly, iLy);
-            dz = min_img(dz, Lz, iLz);
-        }
+        if (PBC) min_image_b(dx, dy, dz, B);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const bool inc = MASKED ? (((mask >> k) & 1u) && r2 < rc2) : r2 < rc2;
         float e, fr;
@@ -780,10 +862,9 @@ __device__ __forceinline__ void tile_steps_x2(const float4* __restrict__ se, flo
 // dphi/deps_i = phi_LJ / (2 eps_i)); j-side sums travel with their slot.
 template <int METHOD, bool PBC>
 __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
-                                               float2 li, unsigned mask, int lane, float Lx, float Ly, float Lz,
-                                               float iLx, float iLy, float iLz, float rc2, float alpha, float krf,
-                                               float crf, float3& fi, float3& fj, double& e64, float3& ai,
-                                               float3& aj) {
+                                               float2 li, unsigned mask, int lane, const ImgBox& B, float rc2,
+                                               float alpha, float krf, float crf, float3& fi, float3& fj,
+                                               double& e64, float3& ai, float3& aj) {
     const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
 #pragma unroll 2
@@ -791,11 +872,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
         const float4 pj = sp[k];
         const float2 lj = sl[k];
         float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-        if (PBC) {
-            dx = min_img(dx, Lx, iLx);
-            dy = min_img(dy, Ly, iLy);
-            dz = min_img(dz, Lz, iLz);
-        }
+        if (PBC) min_image_b(dx, dy, dz, B);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const bool inc = ((mask >> k) & 1u) && r2 < rc2;
         const float r2s = inc ? r2 : 1.0f;
@@ -878,8 +955,6 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         const int aux = wd & 0xfffffu, slot = (wd >> 20) & 0x7ffu;
         const bool pbc = wd >> 31;
         const RepDev& R = a.reps[a.block_rep[I]];
-        const float Lx = R.box[0], Ly = R.box[1], Lz = R.box[2];
-        const float iLx = R.ibox[0], iLy = R.ibox[1], iLz = R.ibox[2];
         const bool diff = kind >= ROW_DIFF1, g2 = kind == ROW_DIFF2;
         const float4* P = kind == ROW_STATE2 ? a.posq2 : a.posq;
         const int i = I16 * kHalf + l;
@@ -912,12 +987,16 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
             // the image of j nearest block I's centre is the minimum image for every i of the block
             float4 c, h;
             row_box(a, I, kind, c, h);
-            pj.x = c.x + min_img(pj.x - c.x, Lx, iLx);
-            pj.y = c.y + min_img(pj.y - c.y, Ly, iLy);
-            pj.z = c.z + min_img(pj.z - c.z, Lz, iLz);
-            pi.x = c.x + min_img(pi.x - c.x, Lx, iLx);
-            pi.y = c.y + min_img(pi.y - c.y, Ly, iLy);
-            pi.z = c.z + min_img(pi.z - c.z, Lz, iLz);
+            float jx = pj.x - c.x, jy = pj.y - c.y, jz = pj.z - c.z;
+            float ix = pi.x - c.x, iy = pi.y - c.y, iz = pi.z - c.z;
+            min_image3(jx, jy, jz, R);
+            min_image3(ix, iy, iz, R);
+            pj.x = c.x + jx;
+            pj.y = c.y + jy;
+            pj.z = c.z + jz;
+            pi.x = c.x + ix;
+            pi.y = c.y + iy;
+            pi.z = c.z + iz;
         }
         // atom tiles without per-pair minimum images need no mask: padding j slots
         // are parked far beyond the cutoff.  The variant is the warp's: masked or
@@ -956,30 +1035,30 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
             tile_steps_x2<METHOD, false>(s_buf[w] + 48 * hf, pi, li, lane, 0u, rc2, alpha, krf, crf, fi, fj, e32);
         } else if (adj) {
             if (pbc_w)
-                tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
+                tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2, alpha, krf,
                                              crf, fi, fj, e64, ai, aj);
             else
-                tile_steps_adj<METHOD, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2, alpha, krf,
+                tile_steps_adj<METHOD, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2, alpha, krf,
                                               crf, fi, fj, e64, ai, aj);
         } else if (diff) {
             if (pbc_w)
-                tile_steps<METHOD, true, true, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, true, true, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                      alpha, krf, crf, fi, fj, e32, e64);
             else if (masked)
-                tile_steps<METHOD, false, true, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, false, true, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                       alpha, krf, crf, fi, fj, e32, e64);
             else
-                tile_steps<METHOD, false, true, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, false, true, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                        alpha, krf, crf, fi, fj, e32, e64);
         } else {
             if (pbc_w)
-                tile_steps<METHOD, true, false, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, true, false, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                       alpha, krf, crf, fi, fj, e32, e64);
             else if (masked)
-                tile_steps<METHOD, false, false, true>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, false, false, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                        alpha, krf, crf, fi, fj, e32, e64);
             else
-                tile_steps<METHOD, false, false, false>(spl, sll, pi, li, mask, lane, Lx, Ly, Lz, iLx, iLy, iLz, rc2,
+                tile_steps<METHOD, false, false, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
                                                         alpha, krf, crf, fi, fj, e32, e64);
         }
         __syncwarp();

@@ -145,3 +145,17 @@ def test_system_owns_added_forces():
     with pytest.raises(atm.ATMError):
         sys_.addForce(atm.ATMMetaForce(0.5, 0.5, 0.0, 0.0, 0.0, 200.0, 100.0, 0.0625, 1.0, [1]))
     assert _lib.load().atm_force_destroy(f._h) == 3  # owned by the System
+
+
+def test_box_vectors_must_be_in_reduced_form():
+    """System::setDefaultPeriodicBoxVectors accepts OpenMM's reduced triclinic
+    form a = (ax,0,0), b = (bx,by,0), c = (cx,cy,cz), |bx|, |cx| <= ax/2, |cy| <= by/2."""
+    s = atm.System()
+    s.addParticle(1.0)
+    s.setDefaultPeriodicBoxVectors((3.0, 0, 0), (1.2, 3.0, 0), (-1.4, 1.5, 3.0))  # reduced
+    for a, b, c in [((3.0, 0, 0), (1.6, 3.0, 0), (0, 0, 3.0)),    # |bx| > ax/2
+                    ((3.0, 0, 0), (0, 3.0, 0), (0, 1.6, 3.0)),    # |cy| > by/2
+                    ((3.0, 0.1, 0), (0, 3.0, 0), (0, 0, 3.0)),    # a not along x
+                    ((3.0, 0, 0), (0, 3.0, 0.2), (0, 0, 3.0))]:   # b out of the xy plane
+        with pytest.raises(atm.ATMError):
+            s.setDefaultPeriodicBoxVectors(a, b, c)

@@ -67,7 +67,14 @@ def check_case(case, diff):
     assert abs(st.getPotentialEnergy() - ref["energy"]) <= tol, (st.getPotentialEnergy(), ref["energy"], tol)
     r = st.getResults()
     assert r["status"] == 0
-    assert abs(r["sp"] - ref["sp"]) <= 1e-6 * max(1.0, abs(ref["sp"]))
+    # sp is the FP64 merge of the record's own energies, and it moves with u: it is
+    # held to the u tolerance times its slope dsp/du (central difference of the merge)
+    m = O.atm_merge(r["E1"], r["E2"], case.params)
+    assert abs(r["sp"] - m["sp"]) <= 1e-9 * max(1.0, abs(m["sp"]))
+    h = 1e-3
+    slope = abs(O.atm_merge(ref["E1"], ref["E2"] + h, case.params)["sp"] -
+                O.atm_merge(ref["E1"], ref["E2"] - h, case.params)["sp"]) / (2 * h)
+    assert abs(r["sp"] - ref["sp"]) <= 2 * slope * U_TOL + 1e-9, (r["sp"], ref["sp"], slope)
     return ctx, f, st, ref
 
 
@@ -85,6 +92,42 @@ def test_nonperiodic_methods(method, diff):
     c = S.water_ligand_box(2394, 3.0, [24], [(1.5, 1.5, 1.5)], method, 0.9, seed=5,
                            params=S.default_params(0.4, 0.6, 0.05, 10.0, 0.0))
     check_case(c, diff)
+
+
+TRICLINIC = {"moderate": ((4.0, 3.8, 3.7), (1.2, -1.0, 0.9)), "skewed": ((4.0, 3.8, 3.7), (1.9, 1.8, -1.8))}
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+@pytest.mark.parametrize("shape", list(TRICLINIC), ids=list(TRICLINIC))
+@pytest.mark.parametrize("method", [S.PME, S.CUTOFF_PERIODIC], ids=["pme", "reaction-field"])
+def test_triclinic_boxes(method, shape, diff):
+    """OpenMM's reduced triclinic boxes (System::setDefaultPeriodicBoxVectors):
+    minimum images c, then b, then a; PME in fractional coordinates."""
+    box, tilt = TRICLINIC[shape]
+    c = S.triclinic_water_ligand_box(5500, box, tilt, [16], [(1.6, 1.5, 1.4)], method, 0.9, seed=13,
+                                     params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
+    check_case(c, diff)
+
+
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_small_triclinic_box_with_per_pair_images(diff):
+    """A box so small against the cutoff that pairs take their own images (the
+    list building searches the 125 images around the blocks' minimum image)."""
+    c = S.triclinic_water_ligand_box(1500, (2.6, 2.5, 2.4), (0.8, -0.7, 0.6), [10], [(1.2, 1.1, 1.0)], S.PME, 0.9,
+                                     seed=14, params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
+    check_case(c, diff)
+
+
+def test_batch_of_triclinic_and_orthorhombic_replicas():
+    cases = [S.triclinic_water_ligand_box(5500, (4.0, 3.8, 3.7), (1.2, -1.0, 0.9), [16], [(1.6, 1.5, 1.4)], S.PME,
+                                          0.9, seed=15),
+             S.water_ligand_box(5000, 3.7, [16], [(1.6, 1.5, 1.4)], S.PME, 0.9, seed=16)]
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    E, F, res = b.evaluate(np.concatenate([c.pos for c in cases]))
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        assert abs(res[k]["pert"] - ref["usc"]) <= U_TOL, k
+        assert force_rel(F[b.offsets[k]:b.offsets[k + 1]], ref["forces"]) <= F_TOL, k
 
 
 @pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
