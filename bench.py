@@ -28,12 +28,15 @@ sys.path.insert(0, os.path.join(ROOT, "openmm-atmmetaforce-plugin_gb300"))
 METRIC = "ATM evals/sec/replica at 23.5k-atom PME: batched vs plain on one GB300 at fixed error"
 F_PAIR = 55.0  # FP32 flops per pair (accounting constant)
 L2_BYTES = 129 * 1024 * 1024
-# DRAM bytes (read + write) of one k_tiles launch on this workload, from an ncu
-# --set full capture (92.53 MB read + 6.08 MB write)
-TILES_TRAFFIC_BYTES = 98.62e6
+# DRAM bytes (read + write) of one k_tiles launch on this workload, from a
+# one-launch ncu --set full capture of the pair-tile kernel at commit 85872e6
+# (92.57 MB read + 6.83 MB write; profiles/k_tiles_abfe-pme-23558x22.md)
+TILES_TRAFFIC_BYTES = 99.40e6
+TILES_CAPTURE = "85872e6"
 # warp instructions of one k_tiles launch on this workload (same capture): the
-# kernel is issue-bound, so its issue rate is the second roofline reported
-TILES_WARP_INSTR = 431.7e6
+# kernel is bound by instruction issue and load latency, so its issue rate is the
+# second roofline reported
+TILES_WARP_INSTR = 347.2e6
 
 
 def parse():
@@ -416,7 +419,7 @@ def main():
     roofline = {"bound": "fp32", "kernel": "k_tiles (pair tiles)", "achieved": achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": TILES_TRAFFIC_BYTES,
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_tiles launch, ncu --set full "
-                                  "capture of this workload (bytes per launch)",
+                                  f"capture of this workload at commit {TILES_CAPTURE} (bytes per launch)",
                 "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
@@ -426,7 +429,8 @@ def main():
                           "peak": props.multi_processor_count * 4 * sm_mhz * 1e6 / 1e12,
                           "unit": "T warp instructions/s",
                           "frac": TILES_WARP_INSTR / t_tiles / (props.multi_processor_count * 4 * sm_mhz * 1e6),
-                          "source": "instructions per launch from the ncu capture, kernel time live"}}
+                          "source": f"instructions per launch from the ncu capture at commit {TILES_CAPTURE}, "
+                                    "kernel time live"}}
 
     md = None
     if not args.no_md:

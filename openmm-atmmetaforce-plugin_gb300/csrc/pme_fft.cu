@@ -53,6 +53,38 @@ __device__ __forceinline__ float2 twid(const float2* tw, int t) {
     return INV ? make_float2(w.x, -w.y) : w;
 }
 
+// Asynchronous global -> shared copies (cp.async): every load of a CTA's input
+// is in flight at once, and none occupies registers while it is.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+// Waits for this thread's copies; a __syncthreads() then publishes them to the CTA.
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Compensated FP32 sum (Knuth's TwoSum): s + c carries the exact sum of the
+// terms up to a relative error of order 2^-48, with FP32 instructions only (the
+// FP64 pipe of this part is narrow).
+__device__ __forceinline__ void two_sum_add(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+}
+
 // Small DFTs in registers, sign -1 (forward) or +1 (INV).
 template <bool INV>
 __device__ __forceinline__ void dft2(float2* v) {
@@ -160,22 +192,23 @@ struct FastDiv {
 // writes its R outputs to (j / Ns) Ns R + k + r Ns.  Work items run
 // sequence-fastest: neighbouring threads take neighbouring sequences, whose
 // starts the callers space by an odd number of words' pairs (no bank conflicts).
-template <int R, bool INV>
+// TW = false: the first stage (Ns = 1), whose twiddles are all 1.
+template <int R, bool INV, bool TW>
 __device__ __forceinline__ void stage_r(const float2* src, float2* dst, const FftStage& p, const FastDiv& fq,
                                         int ss, int es, const float2* tw) {
-    const int nb = p.nb, Ns = p.Ns, step = p.step;
+    const int nb = p.nb, Ns = TW ? p.Ns : 1, step = p.step;
     const int items = nb * (int)fq.d;
     const FastDiv fns((unsigned)Ns, p.mNs);
     for (int w = threadIdx.x; w < items; w += blockDim.x) {
         const int j = (int)fq.div((unsigned)w), q = w - j * (int)fq.d;
-        const int jn = (int)fns.div((unsigned)j);
+        const int jn = TW ? (int)fns.div((unsigned)j) : j;
         const int k = j - jn * Ns;
         const float2* s = src + q * ss;
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const float2 x = s[(j + r * nb) * es];
-            v[r] = r == 0 ? x : cmul(x, twid<INV>(tw, r * k * step));
+            v[r] = (r == 0 || !TW) ? x : cmul(x, twid<INV>(tw, r * k * step));
         }
         if constexpr (R == 2) dft2<INV>(v);
         else if constexpr (R == 4) dft4<INV>(v);
@@ -225,14 +258,26 @@ __device__ int fft_seqs(const Args& a, int plan, float2* buf0, float2* buf1, int
         const FftStage p = st[k];
         const float2* src = cur ? buf1 : buf0;
         float2* dst = cur ? buf0 : buf1;
-        switch (p.R) {
-            case 8: stage_r<8, INV>(src, dst, p, fq, ss, es, tw); break;
-            case 4: stage_r<4, INV>(src, dst, p, fq, ss, es, tw); break;
-            case 2: stage_r<2, INV>(src, dst, p, fq, ss, es, tw); break;
-            case 3: stage_r<3, INV>(src, dst, p, fq, ss, es, tw); break;
-            case 5: stage_r<5, INV>(src, dst, p, fq, ss, es, tw); break;
-            case 7: stage_r<7, INV>(src, dst, p, fq, ss, es, tw); break;
-            default: stage_generic<INV>(src, dst, p, N, fq, ss, es, tw); break;
+        if (p.Ns == 1) {
+            switch (p.R) {
+                case 8: stage_r<8, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                case 4: stage_r<4, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                case 2: stage_r<2, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                case 3: stage_r<3, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                case 5: stage_r<5, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                case 7: stage_r<7, INV, false>(src, dst, p, fq, ss, es, tw); break;
+                default: stage_generic<INV>(src, dst, p, N, fq, ss, es, tw); break;
+            }
+        } else {
+            switch (p.R) {
+                case 8: stage_r<8, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                case 4: stage_r<4, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                case 2: stage_r<2, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                case 3: stage_r<3, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                case 5: stage_r<5, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                case 7: stage_r<7, INV, true>(src, dst, p, fq, ss, es, tw); break;
+                default: stage_generic<INV>(src, dst, p, N, fq, ss, es, tw); break;
+            }
         }
         __syncthreads();
         cur ^= 1;
@@ -247,7 +292,7 @@ __device__ __forceinline__ int zrow(int K2) { return K2 | 1; }
 // Twiddle tables of the three grid dimensions of a replica, copied to shared memory.
 __device__ __forceinline__ void load_tw(const Args& a, const RepDev& R, int d, float2* out) {
     const float2* t = a.fft_tw + R.tw_off[d];
-    for (int k = threadIdx.x; k < R.K[d]; k += blockDim.x) out[k] = t[k];
+    for (int k = threadIdx.x; k < R.K[d]; k += blockDim.x) cp_async8(out + k, t + k);
 }
 
 // Shared memory of the plane kernels: two buffers of a plane of the larger of
@@ -261,7 +306,7 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
     const int K0 = R.K[0], K1 = R.K[1], K2 = R.K[2], K2h = K2 / 2 + 1, P = (K1 + 1) / 2;
     const int g = pc.y / K0, ix = pc.y - g * K0;
     const int zs = zrow(K2);
-    const int plane = max(P * zs, K1 * K2h);
+    const int plane = (max(P * zs, K1 * K2h) + 1) & ~1;  // even: b1 starts on 16 bytes
     float2* b0 = sh;
     float2* b1 = sh + plane;
     float2* tw1 = sh + 2 * plane;
@@ -269,30 +314,23 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
     load_tw(a, R, 1, tw1);
     load_tw(a, R, 2, tw2);
     const float* G = a.qreal + R.real_off + (size_t)g * K0 * K1 * K2 + (size_t)ix * K1 * K2;
-    // rows 2p and 2p + 1 as the real and imaginary parts of row p
-    if ((K2 & 3) == 0) {
-        const int q4 = K2 >> 2;
-        const FastDiv f4(q4);
-        const float4* G4 = reinterpret_cast<const float4*>(G);
-#pragma unroll 2
-        for (int w = threadIdx.x; w < P * q4; w += blockDim.x) {
-            const int p = (int)f4.div((unsigned)w), z4 = w - p * q4;
-            const float4 re = G4[(2 * p) * q4 + z4];
-            const float4 im = 2 * p + 1 < K1 ? G4[(2 * p + 1) * q4 + z4] : make_float4(0.f, 0.f, 0.f, 0.f);
-            float2* d = b0 + p * zs + 4 * z4;
-            d[0] = make_float2(re.x, im.x);
-            d[1] = make_float2(re.y, im.y);
-            d[2] = make_float2(re.z, im.z);
-            d[3] = make_float2(re.w, im.w);
-        }
+    // the real plane as it lies in memory, into b1 (K1 K2 floats <= 2 P zs)
+    float* raw = reinterpret_cast<float*>(b1);
+    if ((K2 & 3) == 0 && ((reinterpret_cast<size_t>(G) | reinterpret_cast<size_t>(raw)) & 15) == 0) {
+        const int n4 = (K1 * K2) >> 2;
+        for (int w = threadIdx.x; w < n4; w += blockDim.x) cp_async16(raw + 4 * w, G + 4 * w);
     } else {
-        const FastDiv fz(K2);
-        for (int w = threadIdx.x; w < P * K2; w += blockDim.x) {
-            const int p = (int)fz.div((unsigned)w), z = w - p * K2;
-            const float re = G[(size_t)(2 * p) * K2 + z];
-            const float im = 2 * p + 1 < K1 ? G[(size_t)(2 * p + 1) * K2 + z] : 0.f;
-            b0[p * zs + z] = make_float2(re, im);
-        }
+        for (int w = threadIdx.x; w < K1 * K2; w += blockDim.x) cp_async4(raw + w, G + w);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // rows 2p and 2p + 1 as the real and imaginary parts of row p
+    const FastDiv fz(K2);
+    for (int w = threadIdx.x; w < P * K2; w += blockDim.x) {
+        const int p = (int)fz.div((unsigned)w), z = w - p * K2;
+        const float re = raw[(2 * p) * K2 + z];
+        const float im = 2 * p + 1 < K1 ? raw[(2 * p + 1) * K2 + z] : 0.f;
+        b0[p * zs + z] = make_float2(re, im);
     }
     __syncthreads();
     const int cz = fft_seqs<false>(a, R.fft_plan[2], b0, b1, K2, P, zs, 1, tw2);
@@ -326,7 +364,7 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
     const int K0 = R.K[0], K1 = R.K[1], K2 = R.K[2], K2h = K2 / 2 + 1, P = (K1 + 1) / 2;
     const int g = pc.y / K0, ix = pc.y - g * K0;
     const int zs = zrow(K2);
-    const int plane = max(P * zs, K1 * K2h);
+    const int plane = (max(P * zs, K1 * K2h) + 1) & ~1;  // even: b1 starts on 16 bytes
     float2* b0 = sh;
     float2* b1 = sh + plane;
     float2* tw1 = sh + 2 * plane;
@@ -335,11 +373,11 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_ifft_yz(Args a) {
     load_tw(a, R, 2, tw2);
     const float2* in = a.qcplx + R.cplx_off + (size_t)g * K0 * K1 * K2h + (size_t)ix * K2h;
     const FastDiv fh(K2h);
-#pragma unroll 4
     for (int w = threadIdx.x; w < K1 * K2h; w += blockDim.x) {
         const int y = (int)fh.div((unsigned)w), kz = w - y * K2h;
-        b0[w] = in[(size_t)y * K0 * K2h + kz];
+        cp_async8(b0 + w, in + (size_t)y * K0 * K2h + kz);
     }
+    cp_async_wait_all();
     __syncthreads();
     const int cy = fft_seqs<true>(a, R.fft_plan[1], b0, b1, K1, K2h, 1, K2h, tw1);
     const float2* S = cy ? b1 : b0;
@@ -398,35 +436,42 @@ __global__ void __launch_bounds__(kFftThreads, 4) k_fft_x_conv(Args a) {
     float2* b0 = sh;
     float2* b1 = sh + K0 * W;
     float2* tw0 = sh + 2 * K0 * W;
+    float* gsh = reinterpret_cast<float*>(tw0 + K0);  // the influence function of the slab, [x][c]
     load_tw(a, R, 0, tw0);
     const size_t C3 = (size_t)K0 * K1 * K2h;
     float2* slab = a.qcplx + R.cplx_off + (size_t)ky * K0 * K2h + kz0;  // [x][kz] of this ky
+    // the influence function of this slab (k_influence), in the slab's layout
+    const float* Gs = a.influence + R.cplx_off / 2 + (size_t)ky * K0 * K2h + kz0;
     const FastDiv fw(W), fn(nz);
-#pragma unroll 4
     for (int w = threadIdx.x; w < K0 * W; w += blockDim.x) {
         const int x = (int)fw.div((unsigned)w), c = w - x * W;
         const int g = c >= nz, kz = c - g * nz;
-        b0[w] = slab[g * C3 + (size_t)x * K2h + kz];
+        cp_async8(b0 + w, slab + g * C3 + (size_t)x * K2h + kz);
     }
+    for (int w = threadIdx.x; w < K0 * nz; w += blockDim.x) {
+        const int x = (int)fn.div((unsigned)w), c = w - x * nz;
+        cp_async4(gsh + w, Gs + (size_t)x * K2h + c);
+    }
+    cp_async_wait_all();
     __syncthreads();
     int cur = fft_seqs<false>(a, R.fft_plan[0], b0, b1, K0, W, 1, W, tw0);
     float2* M = cur ? b1 : b0;
     // influence function G(m) = exp(-pi^2 m^2 / alpha^2) / (pi V m^2 B(m)), B the
-    // B-spline moduli; the half spectrum counts kz in (0, K2/2) twice
-    // the influence function of this slab (k_influence), in the slab's layout
-    const float* Gs = a.influence + R.cplx_off / 2 + (size_t)ky * K0 * K2h + kz0;
-    double ea = 0.0, eb = 0.0;
+    // B-spline moduli; the half spectrum counts kz in (0, K2/2) twice.  Each
+    // thread's terms are summed exactly to about 2^-48 (TwoSum), then in FP64.
+    float sa = 0.f, ca = 0.f, sb = 0.f, cb = 0.f;
 #pragma unroll 2
     for (int w = threadIdx.x; w < K0 * nz; w += blockDim.x) {
         const int x = (int)fn.div((unsigned)w), c = w - x * nz, kz = kz0 + c;
-        const float G = Gs[(size_t)x * K2h + c];
+        const float G = gsh[w];
         const float wgt = (kz == 0 || 2 * kz == K2) ? 1.0f : 2.0f;
         const float2 qa = M[x * W + c], qb = M[x * W + nz + c];
-        ea += (double)(0.5f * wgt * G * (qa.x * qa.x + qa.y * qa.y));
-        eb += (double)(wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y)));
+        two_sum_add(sa, ca, 0.5f * wgt * G * (qa.x * qa.x + qa.y * qa.y));
+        two_sum_add(sb, cb, wgt * G * (qa.x * qb.x + qa.y * qb.y + 0.5f * (qb.x * qb.x + qb.y * qb.y)));
         M[x * W + c] = cscale(qa, G);
         M[x * W + nz + c] = a.full ? cscale(cadd(qa, qb), G) : cscale(qb, G);
     }
+    double ea = (double)sa + (double)ca, eb = (double)sb + (double)cb;
     // fixed-order FP64 sums of the energies: warps, then the CTA
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -492,7 +537,7 @@ void launch_influence(float* G, const float* moduli, const int* mod_off, const i
 
 int fft_plane_smem_bytes(int K1, int K2) {
     const int P = (K1 + 1) / 2, K2h = K2 / 2 + 1, zs = K2 | 1;
-    const int plane = P * zs > K1 * K2h ? P * zs : K1 * K2h;
+    const int plane = ((P * zs > K1 * K2h ? P * zs : K1 * K2h) + 1) & ~1;
     return (int)sizeof(float2) * (2 * plane + K1 + K2);
 }
 
@@ -521,7 +566,9 @@ int fft_plan_stages(int N, std::vector<FftStage>& out) {
     return first | (int)rad.size() << 24;
 }
 
-int fft_conv_smem_bytes(int K0, int nz) { return (int)sizeof(float2) * (2 * K0 * 2 * nz + K0); }
+int fft_conv_smem_bytes(int K0, int nz) {
+    return (int)sizeof(float2) * (2 * K0 * 2 * nz + K0) + (int)sizeof(float) * ((K0 * nz + 1) & ~1);
+}
 
 void launch_fft_forward(const Args& a, cudaStream_t s) {
     if (a.fft_plane_ctas <= 0) return;
