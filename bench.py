@@ -318,6 +318,9 @@ def main():
     batch.evaluate(pos_host)  # layout + capacity
     if args.ncu_case:
         # a few evaluations of the benchmarked batch, for a profiler to capture
+        # (with --tune-cache: at the tuning a plain run stored for this GPU)
+        if args.tune_cache:
+            batch.autotune(trials=5, use_cache=True)
         for _ in range(args.ncu_case):
             batch.evaluate(pos_host)
         print(json.dumps({"ncu_case": args.ncu_case, "launches_per_evaluation": batch.launchCount()}), flush=True)

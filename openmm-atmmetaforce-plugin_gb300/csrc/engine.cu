@@ -872,6 +872,7 @@ void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream) {
     tune_pme_stream_ = pme_stream;
     tile_grid_ = sms_ * std::min(std::max(1, tile_per_sm), max_tile_per_sm_);
     A_.tile_dynamic = tile_dynamic();
+    A_.tile_wide = tile_grid_ <= 3 * sms_ ? 1 : 0;
     if (rebuild && layout_ready_ && method_ == NonbondedForce::PME) {
         build_bricks();
         alloc_device();
@@ -996,6 +997,7 @@ void Engine::alloc_device() {
     a.rcl2 = list_cutoff2();
     a.skin_half2 = (float)(0.25 * skin_ * skin_);
     a.tile_dynamic = tile_dynamic();
+    a.tile_wide = tile_grid_ <= 3 * sms_ ? 1 : 0;
     a.alpha = (float)alpha_;
     a.krf = (float)krf_;
     a.crf = (float)crf_;

@@ -229,6 +229,7 @@ struct Args {
     const uint32_t* masks;    // 16 words per mask (16 x 16 sub-tiles, low 16 bits)
     int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
     int tile_dynamic;         // 1: pair tiles handed out from a counter (large lists)
+    int tile_wide;            // 1: the pair-tile variant budgeted for 3 CTAs per SM (80 registers)
     int* tile_j;              // 32 j slots per tile (atom tiles)
     double* e_tile;           // nrows*row_cap
     double* e_row;            // nrows: sum of each row's tiles

@@ -41,6 +41,32 @@ __device__ __forceinline__ void fix_add_t(unsigned long long* p, float v) {
     atomicAdd(p, fix_bits(v));
 }
 
+// Compensated FP32 sum (Knuth's TwoSum): s + c carries the exact sum of the
+// terms to a relative error of order 2^-48 of their magnitudes, with FP32
+// instructions only (FP64 arithmetic is 1/64 of the FP32 rate on this part).
+__device__ __forceinline__ void two_sum_add(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+}
+
+// Asynchronous global -> shared copies (cp.async), which hold no registers
+// while they are in flight; a warp waits for its own and then __syncwarp()s.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // The box of a replica in registers, for minimum images in the pair loops.
 struct ImgBox {
     float Lx, Ly, Lz, iLx, iLy, iLz, bx, cx, cy;
@@ -666,7 +692,7 @@ template <int METHOD, bool PBC, bool DIFF, bool MASKED>
 __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
                                            float2 li, unsigned mask, int lane, const ImgBox& B, float rc2,
                                            float alpha, float krf, float crf, float3& fi, float3& fj, float& e32,
-                                           double& e64) {
+                                           float2& ec) {
     const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     // the unmasked atom tiles carry most pairs; the other variants stay compact
     // so that the hot loop keeps the instruction cache
@@ -689,7 +715,7 @@ __device__ __forceinline__ void tile_steps(const float4* __restrict__ sp, const 
             e = inc ? e : 0.0f;
             fr = inc ? fr : 0.0f;
         }
-        if (DIFF) e64 += (double)e;
+        if (DIFF) two_sum_add(ec.x, ec.y, e);
         else e32 += e;
         fi.x = fmaf(-fr, dx, fi.x);
         fi.y = fmaf(-fr, dy, fi.y);
@@ -864,7 +890,7 @@ template <int METHOD, bool PBC>
 __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, const float2* __restrict__ sl, float4 pi,
                                                float2 li, unsigned mask, int lane, const ImgBox& B, float rc2,
                                                float alpha, float krf, float crf, float3& fi, float3& fj,
-                                               double& e64, float3& ai, float3& aj) {
+                                               float2& ec, float3& ai, float3& aj) {
     const int src = (lane & kHalf) | ((lane + 1) & (kHalf - 1));  // next lane of this half
     const float inv_ei = li.y > 0.f ? 2.0f / (li.y * li.y) : 0.f;
 #pragma unroll 2
@@ -894,7 +920,7 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
             fr += pi.w * pj.w * (invr * invr2 - 2.0f * krf);
         }
         const float on = inc ? 1.0f : 0.0f;
-        e64 += (double)(on * (elj + pi.w * pj.w * gq));
+        two_sum_add(ec.x, ec.y, on * (elj + pi.w * pj.w * gq));
         fr *= on;
         const float inv_ej = lj.y > 0.f ? 2.0f / (lj.y * lj.y) : 0.f;
         ai.x += on * gq * pj.w;
@@ -913,12 +939,22 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
     }
 }
 
-template <int METHOD, bool DYN>
-__global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
+// MINB: CTAs per SM the registers are budgeted for: 4 (64 registers, some spills
+// around the pair loop) or 3 (80 registers, none); the autotuner's CTAs per SM
+// pick the variant.
+template <int METHOD, bool DYN, int MINB>
+__global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
     // per warp: the j data of its two half tiles, either doubled (64 float4
     // positions + 64 float2 LJ pairs) or in the packed layout (2 x 16 entries of 3
     // float4), 1536 bytes either way
     __shared__ float4 s_buf[kTileThreads / 32][96];
+    // per warp: the next pass's tile entries (one per half) and j slots, copied
+    // asynchronously while the current pass runs (no registers held across its
+    // pair loop), and each lane's bookkeeping for the force and energy output
+    // after the loop: (i, j or -1, energy slot, kind | flags)
+    __shared__ int4 s_next_t[kTileThreads / 32][2];
+    __shared__ int s_next_j[kTileThreads / 32][32];
+    __shared__ int4 s_meta[kTileThreads / 32][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int hf = lane >> 4, l = lane & (kHalf - 1);  // half of the warp, lane within it
     int ntiles = a.status->tile_count;
@@ -936,17 +972,20 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
     while (cur < npairs) {
     if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
     const int cur_end = DYN ? min(cur + kTileGrab, npairs) : cur + 1;
-    // the tile entry and the j slot of the next pass are loaded before this
+    // the tile entry and the j slot of the next pass are copied before this
     // pass's pair loop, so that their latency is hidden behind it
-    int4 Tn = a.tiles[2 * cur + hf];
-    int jn = a.tile_j[(size_t)(2 * cur + hf) * kHalf + l];
+    if (l == 0) cp_async16(&s_next_t[w][hf], a.tiles + 2 * cur + hf);
+    cp_async4(&s_next_j[w][lane], a.tile_j + (size_t)(2 * cur + hf) * kHalf + l);
     for (int pq = cur; pq < cur_end; pq++) {
         const int t = 2 * pq + hf;
-        const int4 T = Tn;
-        const int jraw = jn;
+        cp_async_wait_all();
+        __syncwarp();
+        const int4 T = s_next_t[w][hf];
+        const int jraw = s_next_j[w][lane];
+        __syncwarp();
         if (pq + 1 < cur_end) {
-            Tn = a.tiles[t + 2];
-            jn = a.tile_j[(size_t)(t + 2) * kHalf + l];
+            if (l == 0) cp_async16(&s_next_t[w][hf], a.tiles + t + 2);
+            cp_async4(&s_next_j[w][lane], a.tile_j + (size_t)(t + 2) * kHalf + l);
         }
         const int I16 = T.x, I = I16 >> 1;
         const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
@@ -1025,8 +1064,14 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
         float3 ai = make_float3(0.f, 0.f, 0.f), aj = make_float3(0.f, 0.f, 0.f);
         float e32 = 0.f;
-        double e64 = 0.0;
+        float2 ec = make_float2(0.f, 0.f);  // difference tiles: compensated sum
         const bool adj = diff && a.adjoint;
+        {
+            const bool diag0 = !atom_tile && T.y == I16;
+            const bool skip = atom_tile && aux == 0;  // an empty tile, the filler of an odd row
+            s_meta[w][lane] = make_int4(i, (diag0 || !jvalid) ? -1 : j, row * a.row_cap + slot,
+                                        kind | (skip ? 4 : 0) | (adj ? 8 : 0) | (diag0 ? 16 : 0));
+        }
         if (packed && masked) {
             // the lane's mask (bit k: slot (l + k) & 15) rotated to slot order (bit s: slot s)
             const unsigned sm = ((mask << l) | (mask >> (kHalf - l))) & 0xffffu;
@@ -1036,73 +1081,81 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
         } else if (adj) {
             if (pbc_w)
                 tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2, alpha, krf,
-                                             crf, fi, fj, e64, ai, aj);
+                                             crf, fi, fj, ec, ai, aj);
             else
                 tile_steps_adj<METHOD, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2, alpha, krf,
-                                              crf, fi, fj, e64, ai, aj);
+                                              crf, fi, fj, ec, ai, aj);
         } else if (diff) {
             if (pbc_w)
                 tile_steps<METHOD, true, true, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                     alpha, krf, crf, fi, fj, e32, e64);
+                                                     alpha, krf, crf, fi, fj, e32, ec);
             else if (masked)
                 tile_steps<METHOD, false, true, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                      alpha, krf, crf, fi, fj, e32, e64);
+                                                      alpha, krf, crf, fi, fj, e32, ec);
             else
                 tile_steps<METHOD, false, true, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                       alpha, krf, crf, fi, fj, e32, e64);
+                                                       alpha, krf, crf, fi, fj, e32, ec);
         } else {
             if (pbc_w)
                 tile_steps<METHOD, true, false, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                      alpha, krf, crf, fi, fj, e32, e64);
+                                                      alpha, krf, crf, fi, fj, e32, ec);
             else if (masked)
                 tile_steps<METHOD, false, false, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                       alpha, krf, crf, fi, fj, e32, e64);
+                                                       alpha, krf, crf, fi, fj, e32, ec);
             else
                 tile_steps<METHOD, false, false, false>(spl, sll, pi, li, mask, lane, img_box(R), rc2,
-                                                        alpha, krf, crf, fi, fj, e32, e64);
+                                                        alpha, krf, crf, fi, fj, e32, ec);
         }
         __syncwarp();
-        const bool diag = !atom_tile && T.y == I16;
-        // tile energy over the half, in a fixed order: FP64 on the difference tiles
-        // (their sum is u); FP32 on the state tiles (FP64 arithmetic is scarce on
-        // this part).  In the two-state mode the state-1 and state-2 tiles of atoms
-        // that do not move are the same tiles with the same bits (their j lists
-        // differ only in the moving atoms, which come last), so their FP32 sums
-        // cancel exactly in u = E2 - E1, which the FP64 row and replica sums carry.
-        double esum;
-        if (diff) {
-            esum = e64;
+        // the lane's bookkeeping, kept in shared memory across the pair loop
+        const int4 m = s_meta[w][lane];
+        const int mi = m.x, mj = m.y, mkind = m.w & 3;
+        const bool mdiff = mkind >= ROW_DIFF1, mskip = m.w & 4, madj = m.w & 8, mdiag = m.w & 16;
+        // tile energy over the half, in a fixed order: compensated FP32 (TwoSum) on
+        // the difference tiles (their sum is u), converted to FP64 once per tile;
+        // plain FP32 on the state tiles.  In the two-state mode the state-1 and
+        // state-2 tiles of atoms that do not move are the same tiles with the same
+        // bits (their j lists differ only in the moving atoms, which come last), so
+        // their FP32 sums cancel exactly in u = E2 - E1, which the FP64 row and
+        // replica sums carry.
+        const float sign = mkind == ROW_DIFF1 ? -1.0f : 1.0f;
+        if (mdiff) {
+            float es = ec.x, ce = ec.y;
 #pragma unroll
-            for (int o = kHalf / 2; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL_MASK, esum, o);
+            for (int o = kHalf / 2; o > 0; o >>= 1) {
+                const float s2 = __shfl_xor_sync(FULL_MASK, es, o), c2 = __shfl_xor_sync(FULL_MASK, ce, o);
+                const float t2 = es + s2, bp = t2 - es;
+                ce = (ce + c2) + ((es - (t2 - bp)) + (s2 - bp));
+                es = t2;
+            }
+            if (l == 0) a.e_tile[m.z] = (double)sign * ((double)es + (double)ce);
         } else {
-            float es = diag ? 0.5f * e32 : e32;
+            float es = mdiag ? 0.5f * e32 : e32;
 #pragma unroll
             for (int o = kHalf / 2; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
-            esum = (double)es;
+            if (l == 0) a.e_tile[m.z] = (double)es;
         }
-        const float sign = kind == ROW_DIFF1 ? -1.0f : 1.0f;
-        if (l == 0) a.e_tile[(size_t)row * a.row_cap + slot] = kind == ROW_DIFF1 ? -esum : esum;
-        if (!atom_tile || aux > 0) {  // (an empty tile, the filler of an odd row, adds nothing)
-        unsigned long long* Fp = a.F + (kind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
-        fix_add_t(Fp + i, sign * fi.x);
-        fix_add_t(Fp + a.NA + i, sign * fi.y);
-        fix_add_t(Fp + 2 * (size_t)a.NA + i, sign * fi.z);
-        if (!diag && jvalid) {
-            fix_add_t(Fp + j, sign * fj.x);
-            fix_add_t(Fp + a.NA + j, sign * fj.y);
-            fix_add_t(Fp + 2 * (size_t)a.NA + j, sign * fj.z);
-        }
-        if (adj) {
-            unsigned long long* D = a.D;
-            fix_add_t(D + i, sign * ai.x);
-            fix_add_t(D + a.NA + i, sign * ai.y);
-            fix_add_t(D + 2 * (size_t)a.NA + i, sign * ai.z);
-            if (jvalid) {
-                fix_add_t(D + j, sign * aj.x);
-                fix_add_t(D + a.NA + j, sign * aj.y);
-                fix_add_t(D + 2 * (size_t)a.NA + j, sign * aj.z);
+        if (!mskip) {
+            unsigned long long* Fp = a.F + (mkind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);
+            fix_add_t(Fp + mi, sign * fi.x);
+            fix_add_t(Fp + a.NA + mi, sign * fi.y);
+            fix_add_t(Fp + 2 * (size_t)a.NA + mi, sign * fi.z);
+            if (mj >= 0) {
+                fix_add_t(Fp + mj, sign * fj.x);
+                fix_add_t(Fp + a.NA + mj, sign * fj.y);
+                fix_add_t(Fp + 2 * (size_t)a.NA + mj, sign * fj.z);
             }
-        }
+            if (madj) {
+                unsigned long long* D = a.D;
+                fix_add_t(D + mi, sign * ai.x);
+                fix_add_t(D + a.NA + mi, sign * ai.y);
+                fix_add_t(D + 2 * (size_t)a.NA + mi, sign * ai.z);
+                if (mj >= 0) {
+                    fix_add_t(D + mj, sign * aj.x);
+                    fix_add_t(D + a.NA + mj, sign * aj.y);
+                    fix_add_t(D + 2 * (size_t)a.NA + mj, sign * aj.z);
+                }
+            }
         }
     }
     cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : cur + ((gridDim.x * blockDim.x) >> 5);
@@ -1111,22 +1164,30 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_tiles(Args a) {
 
 int tiles_kernel_blocks_per_sm() {
     int n4 = 0, n2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4, true>, kTileThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2, true>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n4, k_tiles<4, true, 4>, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_tiles<2, true, 4>, kTileThreads, 0);
     return n4 < n2 ? n4 : n2;
+}
+
+template <int METHOD, bool DYN>
+static void launch_tiles_m(const Args& a, int grid, cudaStream_t s) {
+    if (a.tile_wide)
+        k_tiles<METHOD, DYN, 3><<<grid, kTileThreads, 0, s>>>(a);
+    else
+        k_tiles<METHOD, DYN, 4><<<grid, kTileThreads, 0, s>>>(a);
 }
 
 void launch_tiles(const Args& a, int grid, cudaStream_t s) {
     if (a.method == 4) {
         if (a.tile_dynamic)
-            k_tiles<4, true><<<grid, kTileThreads, 0, s>>>(a);
+            launch_tiles_m<4, true>(a, grid, s);
         else
-            k_tiles<4, false><<<grid, kTileThreads, 0, s>>>(a);
+            launch_tiles_m<4, false>(a, grid, s);
     } else {
         if (a.tile_dynamic)
-            k_tiles<2, true><<<grid, kTileThreads, 0, s>>>(a);
+            launch_tiles_m<2, true>(a, grid, s);
         else
-            k_tiles<2, false><<<grid, kTileThreads, 0, s>>>(a);
+            launch_tiles_m<2, false>(a, grid, s);
     }
 }
 
