@@ -485,7 +485,9 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32 pairs / i64 fixed-point forces / f64 energies",
+                "vs_baseline": None, "dtype": "f32",
+                "precision": "f32 pair and grid arithmetic, i64 fixed-point force sums, compensated f32 / f64 energy "
+                             "sums, f64 merge",
                 "data": "synthetic (seeded water boxes + ligand chains)",
                 "config": {"workload": f"abfe-pme-23558 x{R}: {R} replicas of 23,558 atoms (7,838 waters + 44-atom "
                                        "ligand), 6.2 nm box, PME rc 0.9 nm tol 5e-4 grid 56^3, 22-state schedule",
@@ -498,7 +500,8 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": batch.launchCount() * args.steps,
-                "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "md": md}
+                "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(), "md": md,
+                "autotune_report": tune_report.strip().splitlines()}
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()

@@ -1056,7 +1056,7 @@ void Engine::alloc_device() {
     a.dxs_ent = dupload(d_allocs_, dxs_ent_);
     a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
     a.tile_j = dalloc<int>(d_allocs_, (size_t)kHalf * tile_cap_);
-    a.e_tile = dalloc<double>(d_allocs_, (size_t)nrows_ * row_cap_);
+    a.e_tile = dalloc<float2>(d_allocs_, (size_t)nrows_ * row_cap_);
     a.e_row = dalloc<double>(d_allocs_, (size_t)nrows_);
     a.status = dalloc<Status>(d_allocs_, 1);
     a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);

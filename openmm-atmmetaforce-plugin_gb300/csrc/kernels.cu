@@ -942,9 +942,12 @@ __global__ void k_rowsum(Args a) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= a.nrows) return;
     const int n = a.row_count[row];
-    const double* e = a.e_tile + (size_t)row * a.row_cap;
+    const float2* e = a.e_tile + (size_t)row * a.row_cap;
     double s = 0.0;
-    for (int k = lane; k < n; k += 32) s += e[k];
+    for (int k = lane; k < n; k += 32) {
+        const float2 v = e[k];
+        s += (double)v.x + (double)v.y;
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
     if (lane == 0) a.e_row[row] = s;

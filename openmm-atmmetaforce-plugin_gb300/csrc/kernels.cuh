@@ -231,7 +231,7 @@ struct Args {
     int tile_dynamic;         // 1: pair tiles handed out from a counter (large lists)
     int tile_wide;            // 1: the pair-tile variant budgeted for 3 CTAs per SM (80 registers)
     int* tile_j;              // 32 j slots per tile (atom tiles)
-    double* e_tile;           // nrows*row_cap
+    float2* e_tile;           // nrows*row_cap: tile energies as (hi, lo) FP32 pairs, summed in FP64 per row
     double* e_row;            // nrows: sum of each row's tiles
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]

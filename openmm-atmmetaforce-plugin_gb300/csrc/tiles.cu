@@ -1112,8 +1112,9 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
         const int mi = m.x, mj = m.y, mkind = m.w & 3;
         const bool mdiff = mkind >= ROW_DIFF1, mskip = m.w & 4, madj = m.w & 8, mdiag = m.w & 16;
         // tile energy over the half, in a fixed order: compensated FP32 (TwoSum) on
-        // the difference tiles (their sum is u), converted to FP64 once per tile;
-        // plain FP32 on the state tiles.  In the two-state mode the state-1 and
+        // the difference tiles (their sum is u), stored as the (hi, lo) pair that the
+        // FP64 row sums add; plain FP32 on the state tiles.  No FP64 instruction
+        // runs in this kernel (FP64 is 1/64 of the FP32 rate on this part).  In the two-state mode the state-1 and
         // state-2 tiles of atoms that do not move are the same tiles with the same
         // bits (their j lists differ only in the moving atoms, which come last), so
         // their FP32 sums cancel exactly in u = E2 - E1, which the FP64 row and
@@ -1128,12 +1129,12 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
                 ce = (ce + c2) + ((es - (t2 - bp)) + (s2 - bp));
                 es = t2;
             }
-            if (l == 0) a.e_tile[m.z] = (double)sign * ((double)es + (double)ce);
+            if (l == 0) a.e_tile[m.z] = make_float2(sign * es, sign * ce);  // exact: sign is +-1
         } else {
             float es = mdiag ? 0.5f * e32 : e32;
 #pragma unroll
             for (int o = kHalf / 2; o > 0; o >>= 1) es += __shfl_xor_sync(FULL_MASK, es, o);
-            if (l == 0) a.e_tile[m.z] = (double)es;
+            if (l == 0) a.e_tile[m.z] = make_float2(es, 0.f);
         }
         if (!mskip) {
             unsigned long long* Fp = a.F + (mkind == ROW_STATE1 ? 0 : 3 * (size_t)a.NA);

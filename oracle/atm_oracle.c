@@ -193,6 +193,7 @@ typedef struct {
     double* dUdq;       /* may be NULL (parameter-derivative mode) */
     double* dUdsig;
     double* dUdeps;
+    int tric;           /* triclinic box: images by the reduced-box rule */
 } direct_job;
 
 static inline double do_pair(const direct_job* J, int i, int j, double* fi_acc, double* fj_acc) {
@@ -203,13 +204,20 @@ static inline double do_pair(const direct_job* J, int i, int j, double* fi_acc, 
         dc[a] = J->pc[3 * j + a] - J->pc[3 * i + a];
         d[a] = J->pos[3 * j + a] - J->pos[3 * i + a];
     }
-    if (per) {
+    if (per && J->tric) {
         /* the same image shift is applied to the evaluation geometry */
         double shift[3];
         image_shift(s, dc, shift);
         for (int a = 0; a < 3; a++) {
             dc[a] -= shift[a];
             d[a] -= shift[a];
+        }
+    } else if (per) {
+        /* orthorhombic: the axes are independent */
+        for (int a = 0; a < 3; a++) {
+            const double shift = s->box[a] * floor(dc[a] / s->box[a] + 0.5);
+            dc[a] -= shift;
+            d[a] -= shift;
         }
     }
     for (int a = 0; a < 3; a++) {
@@ -782,7 +790,7 @@ int onb_energy_forces(const onb_t* s, const double* pos, const double* pos_cut, 
     excl_csr ex;
     if (build_excl(s, &ex)) return -2;
     if (forces) memset(forces, 0, sizeof(double) * 3 * (size_t)s->n);
-    direct_job J = {s, pos, pos_cut ? pos_cut : pos, &ex, forces, NULL, NULL, NULL};
+    direct_job J = {s, pos, pos_cut ? pos_cut : pos, &ex, forces, NULL, NULL, NULL, is_triclinic(s)};
     oterms_t t = {0, 0, 0, 0, 0};
     t.direct = direct_space(&J);
     t.exceptions = exceptions_term(s, pos, forces, NULL, NULL, NULL);
@@ -806,7 +814,7 @@ int onb_param_derivs(const onb_t* s, const double* pos, const double* pos_cut, d
     if (dUdq) memset(dUdq, 0, sizeof(double) * (size_t)s->n);
     if (dUdsig) memset(dUdsig, 0, sizeof(double) * (size_t)s->n);
     if (dUdeps) memset(dUdeps, 0, sizeof(double) * (size_t)s->n);
-    direct_job J = {s, pos, pos_cut ? pos_cut : pos, &ex, NULL, dUdq, dUdsig, dUdeps};
+    direct_job J = {s, pos, pos_cut ? pos_cut : pos, &ex, NULL, dUdq, dUdsig, dUdeps, is_triclinic(s)};
     direct_space(&J);
     /* exceptions with explicit chargeProd do not depend on the particle charges
        except through the PME exclusion correction */
