@@ -408,7 +408,9 @@ def main():
         a, b = count_pairs(c)
         pairs_state1 += a
         pairs_lig += b
-    t_tiles = kt.get("tiles", float("nan")) * 1e-3
+    # the pair-tile kernel, or the fused lists + pair-tile kernel when the autotuner chose it
+    fused = "find_tiles" in kt
+    t_tiles = kt.get("find_tiles" if fused else "tiles", float("nan")) * 1e-3
     flops = (pairs_state1 + pairs_lig) * F_PAIR
     peaks = {}
     try:
@@ -419,16 +421,20 @@ def main():
     props = torch.cuda.get_device_properties(dev)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops / t_tiles / 1e12
-    roofline = {"bound": "fp32", "kernel": "k_tiles (pair tiles)", "achieved": achieved, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": TILES_TRAFFIC_BYTES,
+    roofline = {"bound": "fp32",
+                "kernel": "k_find_tiles (lists + pair tiles, fused)" if fused else "k_tiles (pair tiles)",
+                "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                "traffic": None if fused else TILES_TRAFFIC_BYTES,
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_tiles launch, ncu --set full "
-                                  f"capture of this workload at commit {TILES_CAPTURE} (bytes per launch)",
+                                  f"capture of this workload at commit {TILES_CAPTURE} (bytes per launch)"
+                                  + ("; not captured for the fused kernel" if fused else ""),
                 "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                "(MEASURED_PEAKS holds no FP32 figure)",
                 "algorithmic": f"{pairs_state1 + pairs_lig} pairs within cutoff x {F_PAIR:.0f} flops",
-                "kernel_ms": kt.get("tiles"), "kernel_times_ms": kt, "tile_stats": batch.stats(),
+                "kernel_ms": t_tiles * 1e3, "kernel_times_ms": kt, "tile_stats": batch.stats(),
                 "pair_slot_efficiency": (pairs_state1 + pairs_lig) / max(1, 256 * batch.stats()["tiles"]),
-                "issue": {"achieved": TILES_WARP_INSTR / t_tiles / 1e12,
+                "issue": None if fused else {"achieved": TILES_WARP_INSTR / t_tiles / 1e12,
                           "peak": props.multi_processor_count * 4 * sm_mhz * 1e6 / 1e12,
                           "unit": "T warp instructions/s",
                           "frac": TILES_WARP_INSTR / t_tiles / (props.multi_processor_count * 4 * sm_mhz * 1e6),

@@ -185,7 +185,10 @@ int atm_system_set_position_restraints_periodic(atm_system_t sys, int periodic);
  * full inner evaluations as in ATMMetaForceImpl.cpp:113,116); ListSkin=nm
  * (default 0: the pair lists are built at every evaluation; > 0: built at the
  * cutoff plus the skin and kept until an atom has moved more than half the skin,
- * which the GPU checks at every evaluation). */
+ * which the GPU checks at every evaluation); FusedTiles=0|1 (default 0: the
+ * pair lists and the pair tiles as two kernels; 1: one persistent kernel that
+ * builds each row's lists and evaluates its tiles at once; the autotuner chooses
+ * between them). */
 int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out);
 int atm_context_destroy(atm_context_t ctx);
 /* Context::setPositions (host doubles, n x 3, nm). */
@@ -260,8 +263,9 @@ int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, d
  * atm_md_autotune before the first step),
  * CheckInterval=steps (default 20: the host reads the list status every that
  * many steps instead of after every step, and redoes the steps since the last
- * check if a list build overflowed).  temperature K, friction 1/ps, step_size
- * ps; seed keys the Philox4x32-10 thermostat noise. */
+ * check if a list build overflowed), FusedTiles=0|1 (as for contexts).
+ * temperature K, friction 1/ps, step_size ps; seed keys the Philox4x32-10
+ * thermostat noise. */
 typedef struct atm_md_s* atm_md_t;
 int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const char* properties,
                   double temperature, double friction, double step_size, unsigned long long seed, atm_md_t* out);

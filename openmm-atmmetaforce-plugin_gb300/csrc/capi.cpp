@@ -602,6 +602,7 @@ int atm_context_create(atm_system_t sys, int device, const char* properties, atm
     v.push_back(std::move(spec));
     c->eng.reset(new Engine(std::move(v), device, !diff));
     c->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
+    c->eng->set_fused(prop_bool(props, "FusedTiles", false));
     c->forces.resize(3 * (size_t)c->n);
     c->forces_nb.resize(3 * (size_t)c->n);
     c->results.resize(NUM_RES);
@@ -701,6 +702,7 @@ int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, co
     std::unique_ptr<atm_batch_s> b(new atm_batch_s);
     b->eng.reset(new Engine(std::move(v), device, !diff, adjoint));
     b->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
+    b->eng->set_fused(prop_bool(props, "FusedTiles", false));
     b->results.resize((size_t)NUM_RES * n_replicas);
     b->matrix.resize((size_t)n_replicas * n_replicas);
     *out = b.release();
@@ -932,6 +934,7 @@ int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const
     }
     std::unique_ptr<atm_md_s> m(new atm_md_s);
     m->md.reset(new MDDriver(v, device, !diff, opt));
+    m->md->engine().set_fused(prop_bool(props, "FusedTiles", false));
     *out = m.release();
     API_END
 }

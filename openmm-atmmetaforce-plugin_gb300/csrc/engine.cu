@@ -865,11 +865,13 @@ std::string Engine::tuning_key() const {
     return k.str();
 }
 
-void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream) {
+void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream, bool fused) {
     bool rebuild = brick != tune_brick_;
     tune_tile_per_sm_ = tile_per_sm;
     tune_brick_ = brick;
     tune_pme_stream_ = pme_stream;
+    tune_fused_ = fused;
+    A_.fused = fused ? 1 : 0;
     tile_grid_ = sms_ * std::min(std::max(1, tile_per_sm), max_tile_per_sm_);
     A_.tile_dynamic = tile_dynamic();
     A_.tile_wide = tile_grid_ <= 3 * sms_ ? 1 : 0;
@@ -877,6 +879,13 @@ void Engine::apply_tuning(int tile_per_sm, int brick, bool pme_stream) {
         build_bricks();
         alloc_device();
     }
+    destroy_graphs();
+}
+
+void Engine::set_fused(bool fused) {
+    if (fused == tune_fused_) return;
+    tune_fused_ = fused;
+    A_.fused = fused ? 1 : 0;
     destroy_graphs();
 }
 
@@ -897,9 +906,10 @@ bool Engine::load_tuning() {
         auto tab = line.find('\t');
         if (tab == std::string::npos || line.substr(0, tab) != key) continue;
         std::istringstream v(line.substr(tab + 1));
-        int t, b, s;
+        int t, b, s, fu = 0;
         if (v >> t >> b >> s) {
-            apply_tuning(t, b, s != 0);
+            if (!(v >> fu)) fu = 0;
+            apply_tuning(t, b, s != 0, fu != 0);
             return true;
         }
     }
@@ -916,17 +926,24 @@ std::string Engine::autotune(int trials, bool use_cache) {
     std::ostringstream rep;
     double best = 1e30;
     int bt = max_tile_per_sm_, bb = tune_brick_;
-    bool bs = tune_pme_stream_;
+    bool bs = tune_pme_stream_, bf = tune_fused_;
     const bool pme = method_ == NonbondedForce::PME;
     std::vector<int> bricks = pme ? std::vector<int>{20, 16, 12, 8} : std::vector<int>{tune_brick_};
     std::vector<int> pmes = pme ? std::vector<int>{1, 0} : std::vector<int>{1};
     cudaEvent_t e0, e1;
     CUDA_CHECK(cudaEventCreate(&e0));
     CUDA_CHECK(cudaEventCreate(&e1));
-    for (int t = max_tile_per_sm_; t >= 2 && t >= max_tile_per_sm_ - 2; t--)
+    // separate list and pair-tile kernels at 4, 3, 2 pair-tile CTAs per SM, then the
+    // fused kernel (its CTAs per SM are fixed)
+    std::vector<std::pair<int, bool>> shapes;
+    for (int t = max_tile_per_sm_; t >= 2 && t >= max_tile_per_sm_ - 2; t--) shapes.push_back({t, false});
+    shapes.push_back({max_tile_per_sm_, true});
+    for (const auto& sh : shapes)
         for (int b : bricks)
             for (int s : pmes) {
-                apply_tuning(t, b, s != 0);
+                const int t = sh.first;
+                const bool fu = sh.second;
+                apply_tuning(t, b, s != 0, fu);
                 run(true, nullptr, nullptr);   // uploads the staged positions (buffers may be new)
                 run(false, nullptr, nullptr);  // device graph capture + one warm evaluation
                 CUDA_CHECK(cudaEventRecord(e0, s_main_));
@@ -936,20 +953,26 @@ std::string Engine::autotune(int trials, bool use_cache) {
                 float ms = 0;
                 CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
                 ms /= trials;
-                rep << "tiles/SM=" << t << " brick=" << b << " pme_stream=" << s << " : " << ms << " ms\n";
+                if (fu)
+                    rep << "fused lists+tiles";
+                else
+                    rep << "tiles/SM=" << t;
+                rep << " brick=" << b << " pme_stream=" << s << " : " << ms << " ms\n";
                 if (ms < best) {
                     best = ms;
                     bt = t;
                     bb = b;
                     bs = s != 0;
+                    bf = fu;
                 }
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    apply_tuning(bt, bb, bs);
-    rep << "chosen: tiles/SM=" << bt << " brick=" << bb << " pme_stream=" << bs << " (" << best << " ms)\n";
+    apply_tuning(bt, bb, bs, bf);
+    rep << "chosen: " << (bf ? "fused lists+tiles" : "tiles/SM=" + std::to_string(bt)) << " brick=" << bb
+        << " pme_stream=" << bs << " (" << best << " ms)\n";
     std::ofstream f(cache_path(), std::ios::app);
-    if (f) f << tuning_key() << "\t" << bt << " " << bb << " " << (bs ? 1 : 0) << "\n";
+    if (f) f << tuning_key() << "\t" << bt << " " << bb << " " << (bs ? 1 : 0) << " " << (bf ? 1 : 0) << "\n";
     return rep.str();
 }
 
@@ -998,6 +1021,7 @@ void Engine::alloc_device() {
     a.skin_half2 = (float)(0.25 * skin_ * skin_);
     a.tile_dynamic = tile_dynamic();
     a.tile_wide = tile_grid_ <= 3 * sms_ ? 1 : 0;
+    a.fused = tune_fused_ ? 1 : 0;
     a.alpha = (float)alpha_;
     a.krf = (float)krf_;
     a.crf = (float)crf_;
@@ -1045,6 +1069,7 @@ void Engine::alloc_device() {
     a.bb_h2 = full_ ? dalloc<float4>(d_allocs_, NB_) : nullptr;
     a.row_desc = dupload(d_allocs_, row_desc_);
     a.row_count = dalloc<int>(d_allocs_, nrows_);
+    a.row_tbase = dalloc<int>(d_allocs_, nrows_);
     a.ex_start = dupload(d_allocs_, ex_start_);
     a.ex_ent = dupload(d_allocs_, ex_ent_);
     a.dx_start = dupload(d_allocs_, dx_start_);
@@ -1188,8 +1213,12 @@ void Engine::record(cudaStream_t st, bool host_io) {
         launch_gather(a, ps);
         if (tune_pme_stream_) CUDA_CHECK(cudaEventRecord(ev_join_, s_pme_));
     }
-    launch_find(a, st);
-    launch_tiles(a, tile_grid_, st);
+    if (a.fused) {
+        launch_find_tiles(a, st);
+    } else {
+        launch_find(a, st);
+        launch_tiles(a, tile_grid_, st);
+    }
     if (!pme) launch_exceptions(a, st);
     if (pme && tune_pme_stream_) CUDA_CHECK(cudaStreamWaitEvent(st, ev_join_, 0));
     launch_finalize(a, st);
@@ -1305,10 +1334,15 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             launch_prepare(a, st);
             launch_decide(a, st);
             mark("prepare");
-            launch_find(a, st);
-            mark("find");
-            launch_tiles(a, tile_grid_, st);
-            mark("tiles");
+            if (a.fused) {
+                launch_find_tiles(a, st);
+                mark("find_tiles");
+            } else {
+                launch_find(a, st);
+                mark("find");
+                launch_tiles(a, tile_grid_, st);
+                mark("tiles");
+            }
             launch_exceptions(a, st);
             mark("exceptions");
             if (method_ == NonbondedForce::PME) {

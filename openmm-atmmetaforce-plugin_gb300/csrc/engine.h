@@ -64,6 +64,8 @@ public:
     // atom has moved more than skin / 2 since their build (checked on the device at
     // every evaluation).  0 (the default): lists are built at every evaluation.
     void set_list_skin(double skin);
+    // lists and pair tiles in one persistent kernel (k_find_tiles) or two kernels
+    void set_fused(bool fused);
     void force_build() { force_build_ = true; }
     double list_skin() const { return skin_; }
     // evaluations run and how many of them built the lists (synchronises the device)
@@ -136,7 +138,7 @@ private:
     float list_cutoff2() const;
     void build_bricks();
     std::string tuning_key() const;
-    void apply_tuning(int tile_per_sm, int brick, bool pme_stream);
+    void apply_tuning(int tile_per_sm, int brick, bool pme_stream, bool fused);
     bool load_tuning();
     void alloc_device();
     void free_device();
@@ -174,6 +176,7 @@ private:
     int tune_tile_per_sm_ = 0;     // 0: as many as fit
     int tune_brick_ = 16;          // spreading brick edge (grid points)
     bool tune_pme_stream_ = true;  // PME on its own stream
+    bool tune_fused_ = false;      // lists and pair tiles in one persistent kernel
 
     // host copies of the layout
     std::vector<int> orig_, slot_of_, block_rep_, block_cls_;

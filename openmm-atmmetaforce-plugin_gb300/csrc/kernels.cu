@@ -130,8 +130,8 @@ __global__ void k_decide(Args a) {
         st->tile_count = 0;
         st->overflow = 0;
         st->max_row = 0;
-        st->next_row = 0;
     }
+    st->next_row = 0;  // the fused kernel walks the rows at every evaluation
     st->rebuild = build ? 1 : 0;
     st->disp2 = 0u;
     a.list_counts[0]++;

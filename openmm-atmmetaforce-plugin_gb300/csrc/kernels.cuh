@@ -218,6 +218,7 @@ struct Args {
     // rows and tiles
     const int4* row_desc;     // nrows: (I, kind, replica, part | parts << 8)
     int* row_count;           // nrows
+    int* row_tbase;           // nrows: first tile of each row in the last build
     const int* ex_start;      // NB+1: exclusion tiles of row I (regular rows)
     const int2* ex_ent;       //   (J, mask id)
     const int* dx_start;      // NB+1: cross-class exclusion tiles (difference rows)
@@ -230,6 +231,7 @@ struct Args {
     int4* tiles;              // tile_cap entries, see tiles.cu for the encoding
     int tile_dynamic;         // 1: pair tiles handed out from a counter (large lists)
     int tile_wide;            // 1: the pair-tile variant budgeted for 3 CTAs per SM (80 registers)
+    int fused;                // 1: lists and pair tiles in one persistent kernel (k_find_tiles)
     int* tile_j;              // 32 j slots per tile (atom tiles)
     float2* e_tile;           // nrows*row_cap: tile energies as (hi, lo) FP32 pairs, summed in FP64 per row
     double* e_row;            // nrows: sum of each row's tiles
@@ -282,6 +284,7 @@ void launch_prepare(const Args& a, cudaStream_t s);
 void launch_decide(const Args& a, cudaStream_t s);
 void launch_find(const Args& a, cudaStream_t s);
 void launch_tiles(const Args& a, int grid, cudaStream_t s);
+void launch_find_tiles(const Args& a, cudaStream_t s);
 void launch_exceptions(const Args& a, cudaStream_t s);
 void launch_spread(const Args& a, cudaStream_t s);
 void launch_conv(const Args& a, cudaStream_t s);

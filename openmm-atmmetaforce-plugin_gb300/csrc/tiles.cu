@@ -527,7 +527,10 @@ __device__ __forceinline__ void find_row(const Args& a, int row, int lane, int* 
     int tbase = 0;
     if (lane == 0) tbase = atomicAdd(&a.status->tile_count, n);
     tbase = __shfl_sync(FULL_MASK, tbase, 0);
-    if (lane == 0) a.row_count[row] = n;
+    if (lane == 0) {
+        a.row_count[row] = n;
+        a.row_tbase[row] = tbase;
+    }
     if (n == 0) return;
     if (tbase + n > a.tile_cap) {
         if (lane == 0) atomicOr(&a.status->overflow, 1);
@@ -939,53 +942,41 @@ __device__ __forceinline__ void tile_steps_adj(const float4* __restrict__ sp, co
     }
 }
 
-// MINB: CTAs per SM the registers are budgeted for: 4 (64 registers, some spills
-// around the pair loop) or 3 (80 registers, none); the autotuner's CTAs per SM
-// pick the variant.
-template <int METHOD, bool DYN, int MINB>
-__global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
-    // per warp: the j data of its two half tiles, either doubled (64 float4
-    // positions + 64 float2 LJ pairs) or in the packed layout (2 x 16 entries of 3
-    // float4), 1536 bytes either way
-    __shared__ float4 s_buf[kTileThreads / 32][96];
-    // per warp: the next pass's tile entries (one per half) and j slots, copied
-    // asynchronously while the current pass runs (no registers held across its
-    // pair loop), and each lane's bookkeeping for the force and energy output
-    // after the loop: (i, j or -1, energy slot, kind | flags)
-    __shared__ int4 s_next_t[kTileThreads / 32][2];
-    __shared__ int s_next_j[kTileThreads / 32][32];
-    __shared__ int4 s_meta[kTileThreads / 32][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// A warp's shared-memory areas for the pair tiles: the j data of its two half
+// tiles, either doubled (64 float4 positions + 64 float2 LJ pairs) or in the
+// packed layout (2 x 16 entries of 3 float4), 96 float4 either way; the next
+// pass's tile entries (one per half) and j slots, copied asynchronously while the
+// current pass runs (no registers held across its pair loop); and each lane's
+// bookkeeping for the force and energy output after the loop: (i, j or -1,
+// energy slot, kind | flags).
+struct TileWarpSmem {
+    float4* buf;
+    int4* next_t;
+    int* next_j;
+    int4* meta;
+};
+
+// The pairs of tiles [cur, cur_end) (pair pq: tiles 2 pq and 2 pq + 1, one per
+// half of the warp; both of one row, since every row holds an even number).
+template <int METHOD>
+__device__ __forceinline__ void tile_pairs(const Args& a, int cur, int cur_end, const TileWarpSmem& S) {
+    const int lane = threadIdx.x & 31;
     const int hf = lane >> 4, l = lane & (kHalf - 1);  // half of the warp, lane within it
-    int ntiles = a.status->tile_count;
-    if (ntiles > a.tile_cap) ntiles = a.tile_cap;
-    const int npairs = ntiles >> 1;  // every row holds an even number of tiles
     const float rc2 = a.rc2, alpha = a.alpha, krf = a.krf, crf = a.crf;
-    // A warp takes two consecutive tiles (one per half; the same row).  Large
-    // lists: pairs handed out kTileGrab at a time from a counter (the next grab
-    // requested before the current pairs are processed), so that warps finish
-    // together.  Small lists (a few pairs per warp): warp w takes pairs w, w + nw, ...
-    // (DYN, chosen by the host from the size of the row list)
-    int mine = 0;
-    if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
-    int cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    while (cur < npairs) {
-    if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
-    const int cur_end = DYN ? min(cur + kTileGrab, npairs) : cur + 1;
     // the tile entry and the j slot of the next pass are copied before this
     // pass's pair loop, so that their latency is hidden behind it
-    if (l == 0) cp_async16(&s_next_t[w][hf], a.tiles + 2 * cur + hf);
-    cp_async4(&s_next_j[w][lane], a.tile_j + (size_t)(2 * cur + hf) * kHalf + l);
+    if (l == 0) cp_async16(&S.next_t[hf], a.tiles + 2 * cur + hf);
+    cp_async4(&S.next_j[lane], a.tile_j + (size_t)(2 * cur + hf) * kHalf + l);
     for (int pq = cur; pq < cur_end; pq++) {
         const int t = 2 * pq + hf;
         cp_async_wait_all();
         __syncwarp();
-        const int4 T = s_next_t[w][hf];
-        const int jraw = s_next_j[w][lane];
+        const int4 T = S.next_t[hf];
+        const int jraw = S.next_j[lane];
         __syncwarp();
         if (pq + 1 < cur_end) {
-            if (l == 0) cp_async16(&s_next_t[w][hf], a.tiles + t + 2);
-            cp_async4(&s_next_j[w][lane], a.tile_j + (size_t)(t + 2) * kHalf + l);
+            if (l == 0) cp_async16(&S.next_t[hf], a.tiles + t + 2);
+            cp_async4(&S.next_j[lane], a.tile_j + (size_t)(t + 2) * kHalf + l);
         }
         const int I16 = T.x, I = I16 >> 1;
         const unsigned z = (unsigned)T.z, wd = (unsigned)T.w;
@@ -1048,10 +1039,10 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
         // state rows without per-pair images (both halves) run two pairs per
         // instruction on the packed layout, masked or not
         const bool packed = !diff && !pbc_w;
-        float4* s_p = s_buf[w];
-        float2* s_l = reinterpret_cast<float2*>(s_buf[w] + 64);
+        float4* s_p = S.buf;
+        float2* s_l = reinterpret_cast<float2*>(S.buf + 64);
         if (packed) {
-            store_packed_j(s_buf[w] + 48 * hf, l, pj, lj);
+            store_packed_j(S.buf + 48 * hf, l, pj, lj);
         } else {
             s_p[32 * hf + l] = pj;
             s_p[32 * hf + l + kHalf] = pj;
@@ -1069,15 +1060,15 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
         {
             const bool diag0 = !atom_tile && T.y == I16;
             const bool skip = atom_tile && aux == 0;  // an empty tile, the filler of an odd row
-            s_meta[w][lane] = make_int4(i, (diag0 || !jvalid) ? -1 : j, row * a.row_cap + slot,
+            S.meta[lane] = make_int4(i, (diag0 || !jvalid) ? -1 : j, row * a.row_cap + slot,
                                         kind | (skip ? 4 : 0) | (adj ? 8 : 0) | (diag0 ? 16 : 0));
         }
         if (packed && masked) {
             // the lane's mask (bit k: slot (l + k) & 15) rotated to slot order (bit s: slot s)
             const unsigned sm = ((mask << l) | (mask >> (kHalf - l))) & 0xffffu;
-            tile_steps_x2<METHOD, true>(s_buf[w] + 48 * hf, pi, li, lane, sm, rc2, alpha, krf, crf, fi, fj, e32);
+            tile_steps_x2<METHOD, true>(S.buf + 48 * hf, pi, li, lane, sm, rc2, alpha, krf, crf, fi, fj, e32);
         } else if (packed) {
-            tile_steps_x2<METHOD, false>(s_buf[w] + 48 * hf, pi, li, lane, 0u, rc2, alpha, krf, crf, fi, fj, e32);
+            tile_steps_x2<METHOD, false>(S.buf + 48 * hf, pi, li, lane, 0u, rc2, alpha, krf, crf, fi, fj, e32);
         } else if (adj) {
             if (pbc_w)
                 tile_steps_adj<METHOD, true>(spl, sll, pi, li, mask, lane, img_box(R), rc2, alpha, krf,
@@ -1108,7 +1099,7 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
         }
         __syncwarp();
         // the lane's bookkeeping, kept in shared memory across the pair loop
-        const int4 m = s_meta[w][lane];
+        const int4 m = S.meta[lane];
         const int mi = m.x, mj = m.y, mkind = m.w & 3;
         const bool mdiff = mkind >= ROW_DIFF1, mskip = m.w & 4, madj = m.w & 8, mdiag = m.w & 16;
         // tile energy over the half, in a fixed order: compensated FP32 (TwoSum) on
@@ -1159,7 +1150,98 @@ __global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
             }
         }
     }
-    cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : cur + ((gridDim.x * blockDim.x) >> 5);
+}
+
+// MINB: CTAs per SM the registers are budgeted for: 4 (64 registers, some spills
+// around the pair loop) or 3 (80 registers, none); the autotuner's CTAs per SM
+// pick the variant.
+template <int METHOD, bool DYN, int MINB>
+__global__ void __launch_bounds__(kTileThreads, MINB) k_tiles(Args a) {
+    __shared__ float4 s_buf[kTileThreads / 32][96];
+    __shared__ int4 s_next_t[kTileThreads / 32][2];
+    __shared__ int s_next_j[kTileThreads / 32][32];
+    __shared__ int4 s_meta[kTileThreads / 32][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const TileWarpSmem S{s_buf[w], s_next_t[w], s_next_j[w], s_meta[w]};
+    int ntiles = a.status->tile_count;
+    if (ntiles > a.tile_cap) ntiles = a.tile_cap;
+    const int npairs = ntiles >> 1;  // every row holds an even number of tiles
+    // A warp takes two consecutive tiles (one per half; the same row).  Large
+    // lists: pairs handed out kTileGrab at a time from a counter (the next grab
+    // requested before the current pairs are processed), so that warps finish
+    // together.  Small lists (a few pairs per warp): warp w takes pairs w, w + nw, ...
+    // (DYN, chosen by the host from the size of the row list)
+    int mine = 0;
+    if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+    int cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    while (cur < npairs) {
+        if (DYN && lane == 0) mine = atomicAdd(&a.status->next_tile, kTileGrab);
+        const int cur_end = DYN ? min(cur + kTileGrab, npairs) : cur + 1;
+        tile_pairs<METHOD>(a, cur, cur_end, S);
+        cur = DYN ? __shfl_sync(FULL_MASK, mine, 0) : cur + ((gridDim.x * blockDim.x) >> 5);
+    }
+}
+
+// Lists and pair tiles in one persistent kernel: a warp takes a row (longest
+// first, as k_find), builds its tiles when this evaluation builds the lists, and
+// evaluates them at once, while they are in L1 / L2; with kept lists (a skin) it
+// evaluates the row's tiles of the last build.  The finder's load-latency-bound
+// phases of some warps run beside the issue-bound pair loops of others on the
+// same SM.  Five CTAs of four warps per SM (102 registers, 45 KB of shared memory
+// each).
+constexpr int kFusedMinBlocks = 5;
+
+template <int METHOD, bool TRIC>
+__global__ void __launch_bounds__(kFindWarps * 32, kFusedMinBlocks) k_find_tiles(Args a) {
+    __shared__ int s_stage[kFindWarps][kStageAtoms];
+    __shared__ float4 s_ipos[kFindWarps][32];
+    __shared__ float4 s_buf[kFindWarps][96];
+    __shared__ int4 s_next_t[kFindWarps][2];
+    __shared__ int s_next_j[kFindWarps][32];
+    __shared__ int4 s_meta[kFindWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const TileWarpSmem S{s_buf[w], s_next_t[w], s_next_j[w], s_meta[w]};
+    const bool build = a.status->rebuild != 0;
+    if (build && a.skin_half2 > 0.f)  // the positions of this build, for the displacement test
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.NA; s += gridDim.x * blockDim.x)
+            a.posq_ref[s] = a.posq[s];
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int mine = a.nrows;
+    while (k < a.nrows) {
+        if (lane == 0) mine = nw < a.nrows ? nw + atomicAdd(&a.status->next_row, 1) : a.nrows;
+        const int row = a.nrows - 1 - k;
+        if (build) find_row<TRIC>(a, row, lane, s_stage[w], s_ipos[w]);
+        __syncwarp();
+        // the row's tiles (written by this warp just now, or by an earlier build)
+        const int n = a.row_count[row], tb = a.row_tbase[row];
+        if (n > 0 && tb + n <= a.tile_cap) tile_pairs<METHOD>(a, tb >> 1, (tb + n) >> 1, S);
+        k = __shfl_sync(FULL_MASK, mine, 0);
+    }
+}
+
+void launch_find_tiles(const Args& a, cudaStream_t s) {
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int p4 = 0, p2 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, k_find_tiles<4, true>, kFindWarps * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, k_find_tiles<2, true>, kFindWarps * 32, 0);
+        per_sm = std::max(1, std::min(p4, p2));
+    }
+    const int blocks = std::min(per_sm * sms, (a.nrows + kFindWarps - 1) / kFindWarps);
+    if (a.method == 4) {
+        if (a.any_tric)
+            k_find_tiles<4, true><<<blocks, kFindWarps * 32, 0, s>>>(a);
+        else
+            k_find_tiles<4, false><<<blocks, kFindWarps * 32, 0, s>>>(a);
+    } else {
+        if (a.any_tric)
+            k_find_tiles<2, true><<<blocks, kFindWarps * 32, 0, s>>>(a);
+        else
+            k_find_tiles<2, false><<<blocks, kFindWarps * 32, 0, s>>>(a);
     }
 }
 

@@ -102,6 +102,23 @@ def test_headline_energy_matrix(headline):
         assert np.all(np.abs((M[r] - M[r, 0]) - BETA * (row - row[0])) <= 2 * BETA * U_TOL), r
 
 
+def test_headline_batch_through_the_fused_kernel(headline):
+    """The same batch with the lists and pair tiles in one persistent kernel
+    (FusedTiles=1, which the autotuner may choose): every replica against the
+    oracle, and against the two-kernel path (FP32 pair sums in another order)."""
+    cases, b, E, F, res, refs, M = headline
+    fb = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0, {"DifferencePath": 1, "FusedTiles": 1})
+    E2, F2, res2 = fb.evaluate(np.concatenate([c.pos for c in cases]))
+    assert force_rel(F2, F) <= 1e-5
+    du = []
+    for k, (c, ref) in enumerate(zip(cases, refs)):
+        assert res2[k]["status"] == 0
+        du.append(abs(res2[k]["pert"] - ref["usc"]))
+        assert force_rel(F2[fb.offsets[k]:fb.offsets[k + 1]], ref["forces"]) <= F_TOL, k
+        assert abs(E2[k] - ref["energy"]) <= energy_tol(c.spec, c.pos), k
+    assert max(du) <= U_TOL, du
+
+
 def test_plain_single_replica_at_bench_settings(headline):
     cases, b, E, F, res, refs, M = headline
     c = cases[0]

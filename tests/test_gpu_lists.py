@@ -48,13 +48,14 @@ def force_rel(F, G):
     return float(np.sqrt(((F - G) ** 2).sum() / (G ** 2).sum()))
 
 
+@pytest.mark.parametrize("fused", [0, 1], ids=["two-kernels", "fused"])
 @pytest.mark.parametrize("method,diff", [(S.PME, 1), (S.PME, 0), (S.CUTOFF_PERIODIC, 1)],
                          ids=["pme-difference", "pme-two-states", "rf-difference"])
-def test_kept_lists_give_the_results_of_fresh_ones(method, diff):
+def test_kept_lists_give_the_results_of_fresh_ones(method, diff, fused):
     case = S.water_ligand_box(6000, 3.9, [18], [(1.9, 1.8, 2.0)], method, 0.9, seed=91,
                               params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
     sys_ = atm.system_from_case(case)[0]
-    kept = atm.ReplicaBatch([sys_], 0, {"DifferencePath": diff, "ListSkin": 0.1})
+    kept = atm.ReplicaBatch([sys_], 0, {"DifferencePath": diff, "ListSkin": 0.1, "FusedTiles": fused})
     fresh = atm.ReplicaBatch([atm.system_from_case(case)[0]], 0, {"DifferencePath": diff})
     rng = np.random.default_rng(3)
     p0 = case.pos
@@ -104,9 +105,13 @@ def _md(props, steps, seed=5):
 def test_md_with_kept_lists_follows_the_rebuilt_trajectory():
     a = _md({"ListSkin": 0.0, "CheckInterval": 1}, 60)
     b = _md({"ListSkin": 0.1, "CheckInterval": 10}, 60)
+    c = _md({"ListSkin": 0.1, "CheckInterval": 10, "FusedTiles": 1}, 60)  # lists and tiles in one kernel
     xa = a.getState(getPositions=True).getPositions()
     xb = b.getState(getPositions=True).getPositions()
+    xc = c.getState(getPositions=True).getPositions()
     assert np.abs(xa - xb).max() <= 1e-4
+    assert np.abs(xa - xc).max() <= 1e-4
+    assert c.listInfo()["builds"] < c.listInfo()["evaluations"]
     ib = b.listInfo()
     assert ib["builds"] < ib["evaluations"]  # the lists were kept between builds
     assert a.listInfo()["builds"] == a.listInfo()["evaluations"]

@@ -49,16 +49,16 @@ def energy_tol(spec, pos):
     return 2e-6 * (sum(abs(v) for v in T.values()) + 1.0)
 
 
-def run_context(case, diff, groups=(2,)):
+def run_context(case, diff, groups=(2,), fused=0):
     sys_, nb, f = atm.system_from_case(case)
-    ctx = atm.Context(sys_, 0, {"DifferencePath": int(diff)})
+    ctx = atm.Context(sys_, 0, {"DifferencePath": int(diff), "FusedTiles": int(fused)})
     ctx.setPositions(case.pos)
     st = ctx.getState(getEnergy=True, getForces=True, groups=set(groups))
     return ctx, f, st
 
 
-def check_case(case, diff):
-    ctx, f, st = run_context(case, diff)
+def check_case(case, diff, fused=0):
+    ctx, f, st = run_context(case, diff, fused=fused)
     ref = O.atm_eval(case.spec, case.pos, case.displ, case.params)
     u = f.getPerturbationEnergy(ctx)
     assert abs(u - ref["usc"]) <= U_TOL, (u, ref["usc"])
@@ -107,6 +107,21 @@ def test_triclinic_boxes(method, shape, diff):
     c = S.triclinic_water_ligand_box(5500, box, tilt, [16], [(1.6, 1.5, 1.4)], method, 0.9, seed=13,
                                      params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
     check_case(c, diff)
+
+
+@pytest.mark.parametrize("method", [S.PME, S.CUTOFF_PERIODIC, S.NOCUTOFF], ids=["pme", "reaction-field", "no-cutoff"])
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_fused_lists_and_tiles_kernel(diff, method):
+    """FusedTiles=1: one persistent kernel builds each row's lists and evaluates
+    its tiles, in a triclinic box for the periodic methods."""
+    if method == S.NOCUTOFF:
+        c = S.water_ligand_box(1500, 2.5, [10], [(1.2, 1.1, 1.0)], method, 0.9, seed=17,
+                               params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
+    else:
+        box, tilt = TRICLINIC["skewed"]
+        c = S.triclinic_water_ligand_box(5500, box, tilt, [16], [(1.6, 1.5, 1.4)], method, 0.9, seed=18,
+                                         params=S.default_params(0.3, 0.6, 0.1, 20.0, 0.0))
+    check_case(c, diff, fused=1)
 
 
 @pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
