@@ -335,8 +335,9 @@ int atm_rf_nonbonded_noalloc(int n, const double* d_pos, const double* d_charge,
 
 /* ---- autotuner -------------------------------------------------------------- */
 /* No counterpart in the reference.  Times `trials` evaluations per configuration
- * of the launch space (pair-tile CTAs per SM, PME spreading brick edge 8/12/16/20,
- * PME chain on its own stream or in line) on the stored positions and keeps the
+ * of the launch space (pair-tile CTAs per SM and register variant, the fused
+ * list + pair-tile kernel, PME spreading brick edge 12/16/19/20, PME chain on its
+ * own stream or in line) on the stored positions and keeps the
  * fastest; with use_cache a choice stored for the same GPU and workload (file
  * $ATM_AUTOTUNE_CACHE, else ~/.cache/atm_gb300_autotune.txt) is reused.  The
  * report (one line per configuration) is written to report (nullable). */

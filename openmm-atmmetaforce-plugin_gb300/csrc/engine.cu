@@ -217,6 +217,8 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     CUDA_CHECK(cudaMallocHost(&h_reps_, sizeof(RepDev) * (size_t)R_));
     CUDA_CHECK(cudaMallocHost(&h_beta_, sizeof(double)));
     CUDA_CHECK(cudaMallocHost(&h_ctl_, 2 * sizeof(int)));
+    CUDA_CHECK(cudaMallocHost(&h_io_, 2 * sizeof(double*)));
+    h_io_[0] = h_io_[1] = nullptr;
     CUDA_CHECK(cudaMalloc(&d_counts_, 2 * sizeof(long long)));
     CUDA_CHECK(cudaMemset(d_counts_, 0, 2 * sizeof(long long)));
     h_ctl_[0] = 1;
@@ -248,6 +250,7 @@ Engine::~Engine() {
     cudaFreeHost(h_reps_);
     cudaFreeHost(h_beta_);
     cudaFreeHost(h_ctl_);
+    cudaFreeHost(h_io_);
     if (d_counts_) cudaFree(d_counts_);
     cudaFreeHost(h_status_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
@@ -261,7 +264,8 @@ Engine::~Engine() {
 void Engine::destroy_graphs() {
     if (graph_host_) cudaGraphExecDestroy(graph_host_);
     if (graph_dev_) cudaGraphExecDestroy(graph_dev_);
-    graph_host_ = graph_dev_ = nullptr;
+    if (graph_res_) cudaGraphExecDestroy(graph_res_);
+    graph_host_ = graph_dev_ = graph_res_ = nullptr;
 }
 
 void Engine::set_positions(int r, const double* pos) {
@@ -845,8 +849,10 @@ void Engine::build_bricks() {
         rd.brick_cta_b = (int)brick_cta_rep_.size();
         int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
         for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
-        // int32 accumulator of a brick padded by the stencil reach (4 points) on each side
-        brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + 8) * (rd.bsz[1] + 8) * (rd.bsz[2] + 8)));
+        // int32 accumulator of a brick padded by the stencil reach (4 points) on each
+        // side, z rows at a bank-spreading stride
+        brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + 8) * (rd.bsz[1] + 8) *
+                                                  spread_row_stride(rd.bsz[2] + 8)));
     }
 }
 
@@ -928,7 +934,7 @@ std::string Engine::autotune(int trials, bool use_cache) {
     int bt = max_tile_per_sm_, bb = tune_brick_;
     bool bs = tune_pme_stream_, bf = tune_fused_;
     const bool pme = method_ == NonbondedForce::PME;
-    std::vector<int> bricks = pme ? std::vector<int>{20, 16, 12, 8} : std::vector<int>{tune_brick_};
+    std::vector<int> bricks = pme ? std::vector<int>{20, 19, 16, 12} : std::vector<int>{tune_brick_};
     std::vector<int> pmes = pme ? std::vector<int>{1, 0} : std::vector<int>{1};
     cudaEvent_t e0, e1;
     CUDA_CHECK(cudaEventCreate(&e0));
@@ -1037,6 +1043,11 @@ void Engine::alloc_device() {
     }
     a.slot_of = dupload(d_allocs_, slot_of_);
     a.f_out = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
+    {
+        double** io = dalloc<double*>(d_allocs_, 2);
+        CUDA_CHECK(cudaMemset(io, 0, 2 * sizeof(double*)));
+        a.io = io;
+    }
     a.f_nb = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
     a.orig = dupload(d_allocs_, orig_);
     a.qs = dupload(d_allocs_, qs_);
@@ -1184,8 +1195,9 @@ int Engine::launches_per_eval() const {
     return n;
 }
 
-void Engine::record(cudaStream_t st, bool host_io) {
+void Engine::record(cudaStream_t st, int mode) {
     const Args& a = A_;
+    const bool host_io = mode == 1;
     if (host_io) {
         CUDA_CHECK(cudaMemcpyAsync((void*)a.pos_in, h_pos_, sizeof(double) * 3 * (size_t)n_in_,
                                    cudaMemcpyHostToDevice, st));
@@ -1193,6 +1205,7 @@ void Engine::record(cudaStream_t st, bool host_io) {
     CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemcpyAsync((void*)a.io, h_io_, 2 * sizeof(double*), cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
     launch_prepare(a, st);
     launch_decide(a, st);
@@ -1234,14 +1247,18 @@ void Engine::record(cudaStream_t st, bool host_io) {
         launch_output(a, st);
         launch_matrix(a, st);
     }
-    if (host_io) {
+    // host flavours: the result records and the R x R matrix (a few KB) end the
+    // evaluation in page-locked host memory, so that a host caller needs no copy after it
+    if (mode != 0) {
         CUDA_CHECK(cudaMemcpyAsync(h_results_, a.results, sizeof(double) * NUM_RES * (size_t)R_,
                                    cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(h_matrix_, a.matrix, sizeof(double) * (size_t)R_ * R_, cudaMemcpyDeviceToHost,
+                                   st));
+    }
+    if (host_io) {
         CUDA_CHECK(cudaMemcpyAsync(h_forces_, a.f_out, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost,
                                    st));
         CUDA_CHECK(cudaMemcpyAsync(h_fnb_, a.f_nb, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaMemcpyAsync(h_matrix_, a.matrix, sizeof(double) * (size_t)R_ * R_, cudaMemcpyDeviceToHost,
-                                   st));
     }
     CUDA_CHECK(cudaMemcpyAsync(h_status_, a.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
 }
@@ -1329,6 +1346,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync((void*)a.io, h_io_, 2 * sizeof(double*), cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
             mark("start");
             launch_prepare(a, st);
@@ -1378,12 +1396,13 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             for (auto e : ev) cudaEventDestroy(e);
             times_.erase(times_.begin());
         } else {
-            cudaGraphExec_t& gx = host_io ? graph_host_ : graph_dev_;
+            const int mode = host_io ? 1 : (h_pos_pinned ? 2 : 0);
+            cudaGraphExec_t& gx = mode == 1 ? graph_host_ : (mode == 2 ? graph_res_ : graph_dev_);
             if (!gx) {
                 cudaGraph_t g;
                 CUDA_CHECK(cudaStreamBeginCapture(s_main_, cudaStreamCaptureModeThreadLocal));
                 try {
-                    record(s_main_, host_io);
+                    record(s_main_, mode);
                 } catch (...) {
                     cudaStreamEndCapture(s_main_, &g);
                     throw;
@@ -1414,6 +1433,19 @@ static bool is_pinned(const void* p) {
         return false;
     }
     return at.type == cudaMemoryTypeHost;
+}
+
+// The device address of a page-locked, mapped host buffer (cudaHostAlloc, or
+// cudaHostRegister with mapping), which kernels can write over the host link; null
+// for other memory.
+static double* host_mapped(double* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    return static_cast<double*>(at.devicePointer);
 }
 
 // Host copy split over a few threads (a single core moves ~10-20 GB/s).
@@ -1447,20 +1479,29 @@ void Engine::evaluate_host(const double* pos, double* energies, double* forces, 
     if (profiling_) {
         run(true, nullptr, nullptr);
     } else {
-        // positions straight from a pinned caller buffer, else from the pinned staging copy
-        run(false, s_main_, nullptr, pin_in ? pos : h_pos_);
-        const bool pin_out = forces && is_pinned(forces);
-        cudaStream_t st = s_main_;
-        CUDA_CHECK(cudaMemcpyAsync(h_results_, A_.results, sizeof(double) * NUM_RES * (size_t)R_,
-                                   cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaMemcpyAsync(h_matrix_, A_.matrix, sizeof(double) * (size_t)R_ * R_, cudaMemcpyDeviceToHost,
-                                   st));
-        if (forces)
-            CUDA_CHECK(cudaMemcpyAsync(pin_out ? forces : h_forces_, A_.f_out, bytes, cudaMemcpyDeviceToHost, st));
-        if (forces_nb) CUDA_CHECK(cudaMemcpyAsync(h_fnb_, A_.f_nb, bytes, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
-        if (forces && !pin_out) par_memcpy(forces, h_forces_, bytes);
-        if (forces_nb) par_memcpy(forces_nb, h_fnb_, bytes);
+        // positions straight from a pinned caller buffer, else from the pinned
+        // staging copy; forces written by the output kernel straight into a
+        // page-locked caller buffer over the host link (no copy after the graph)
+        double* zc = forces ? host_mapped(forces) : nullptr;
+        h_io_[1] = zc;
+        try {
+            run(false, s_main_, nullptr, pin_in ? pos : h_pos_);
+        } catch (...) {
+            h_io_[1] = nullptr;
+            throw;
+        }
+        h_io_[1] = nullptr;  // (the graph that read it has finished)
+        const bool copy_f = forces && !zc;
+        if (copy_f || forces_nb) {
+            const bool pin_out = copy_f && is_pinned(forces);
+            cudaStream_t st = s_main_;
+            if (copy_f)
+                CUDA_CHECK(cudaMemcpyAsync(pin_out ? forces : h_forces_, A_.f_out, bytes, cudaMemcpyDeviceToHost, st));
+            if (forces_nb) CUDA_CHECK(cudaMemcpyAsync(h_fnb_, A_.f_nb, bytes, cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            if (copy_f && !pin_out) par_memcpy(forces, h_forces_, bytes);
+            if (forces_nb) par_memcpy(forces_nb, h_fnb_, bytes);
+        }
         forces = nullptr;
         forces_nb = nullptr;
     }

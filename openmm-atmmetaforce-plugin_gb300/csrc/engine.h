@@ -145,7 +145,11 @@ private:
     void upload_static();
     void fill_args();
     void update_rep_table();
-    void record(cudaStream_t main, bool host_io);
+    // graph flavours: 0 device buffers only (MD, torch), 1 host staging copies of
+    // positions, forces and results, 2 results and matrix to the host (positions
+    // copied in before the launch, forces to a page-locked caller buffer or copied
+    // after it)
+    void record(cudaStream_t main, int mode);
     void pme_transforms(cudaStream_t st, const std::function<void(const char*)>& mark = nullptr);
     void run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned = nullptr);
     bool check_status_and_grow();
@@ -226,6 +230,8 @@ private:
     RepDev* h_reps_ = nullptr;     // R
     double* h_beta_ = nullptr;
     int* h_ctl_ = nullptr;         // list control word, copied to the device by every evaluation
+    double** h_io_ = nullptr;      // [1]: page-locked caller buffer for the forces (null: f_out),
+                                   // copied to the device by every evaluation
     Status* h_status_ = nullptr;
 
     // device buffers
@@ -235,7 +241,7 @@ private:
 
     cudaStream_t s_main_ = nullptr, s_pme_ = nullptr;
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr, ev_fork2_ = nullptr, ev_join2_ = nullptr;
-    cudaGraphExec_t graph_host_ = nullptr, graph_dev_ = nullptr;
+    cudaGraphExec_t graph_host_ = nullptr, graph_dev_ = nullptr, graph_res_ = nullptr;
     std::vector<KernelTime> times_;
 };
 

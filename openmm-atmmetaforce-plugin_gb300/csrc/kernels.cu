@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     const bool padded = R.K[0] >= e[0] + 2 * kBrickPad && R.K[1] >= e[1] + 2 * kBrickPad &&
                         R.K[2] >= e[2] + 2 * kBrickPad;
     const int pad = padded ? kBrickPad : 0;
-    const int P0 = e[0] + 2 * pad, P1 = e[1] + 2 * pad, P2 = e[2] + 2 * pad;
+    const int P0 = e[0] + 2 * pad, P1 = e[1] + 2 * pad, P2 = spread_row_stride(e[2] + 2 * pad);
     int* acc = s_dyn;
     float* st = (float*)(s_dyn + a.brick_smem / 4) + warp * 32 * kStencilWords;  // this warp's staged stencils
     for (int k = tid; k < P0 * P1 * P2; k += kBrickThreads) acc[k] = 0;
@@ -1011,30 +1011,54 @@ void launch_finalize(const Args& a, cudaStream_t s) {
     k_finalize<<<a.R, 256, 0, s>>>(a);
 }
 
-// hybrid forces in user order
-__global__ void k_output(Args a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.NA) return;
-    int o = a.orig[s];
-    if (o < 0) return;
-    int rep = a.block_rep[s >> 5];
-    const RepDev& R = a.reps[rep];
-    const double* res = a.results + (size_t)rep * NUM_RES;
-    double sp = res[RES_SP];
-    double w = R.params[8] > 0 ? sp : 1.0 - sp;
-    size_t out = 3 * (size_t)(R.in_off + o);
-    for (int k = 0; k < 3; k++) {
-        long long f1 = (long long)a.F[(size_t)k * a.NA + s];
-        long long f2 = (long long)a.F[(size_t)(3 + k) * a.NA + s];
-        double d = a.full ? (double)(f2 - f1) : (double)f2;
-        double f = R.var_nb ? ((double)f1 + w * d) * (1.0 / kFixScale) : 0.0;
-        a.f_out[out + k] = f;
-        if (a.f_nb) a.f_nb[out + k] = (double)f1 * (1.0 / kFixScale);
+// Hybrid forces in user order: thread g takes input atom g (its slot from
+// slot_of), so that a warp's 32 atoms are 768 contiguous bytes of the output,
+// written as 16-byte words through shared memory.  The output is f_out, or a
+// page-locked host buffer the caller passed (io[1]), written over the host link
+// without a separate copy.
+constexpr int kOutThreads = 256;
+
+__global__ void __launch_bounds__(kOutThreads) k_output(Args a) {
+    __shared__ double s_f[kOutThreads / 32][96];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double* const fo = a.io[1] ? a.io[1] : a.f_out;
+    double f[3] = {0.0, 0.0, 0.0};
+    if (g < a.n_in) {
+        const int s = a.slot_of[g];
+        const int rep = a.block_rep[s >> 5];
+        const RepDev& R = a.reps[rep];
+        const double* res = a.results + (size_t)rep * NUM_RES;
+        const double sp = res[RES_SP];
+        const double wgt = R.params[8] > 0 ? sp : 1.0 - sp;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const long long f1 = (long long)a.F[(size_t)k * a.NA + s];
+            const long long f2 = (long long)a.F[(size_t)(3 + k) * a.NA + s];
+            const double d = a.full ? (double)(f2 - f1) : (double)f2;
+            f[k] = R.var_nb ? ((double)f1 + wgt * d) * (1.0 / kFixScale) : 0.0;
+            if (a.f_nb) a.f_nb[3 * (size_t)g + k] = (double)f1 * (1.0 / kFixScale);
+        }
+    }
+    const int g0 = g - lane;  // the warp's first atom
+    const int nv = min(32, a.n_in - g0);
+    if (nv <= 0) return;
+    double* const dst = fo + 3 * (size_t)g0;
+    if (nv == 32 && (reinterpret_cast<size_t>(dst) & 15) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) s_f[w][3 * lane + k] = f[k];
+        __syncwarp();
+        const double2* src = reinterpret_cast<const double2*>(s_f[w]);
+        double2* d2 = reinterpret_cast<double2*>(dst);
+        d2[lane] = src[lane];
+        if (lane < 16) d2[32 + lane] = src[32 + lane];
+    } else if (lane < nv) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) dst[3 * lane + k] = f[k];
     }
 }
 
 void launch_output(const Args& a, cudaStream_t s) {
-    k_output<<<(a.NA + 255) / 256, 256, 0, s>>>(a);
+    k_output<<<(a.n_in + kOutThreads - 1) / kOutThreads, kOutThreads, 0, s>>>(a);
 }
 
 // replicas x states energy matrix: beta * (e0(r; dir_s) + W_s(usc_s(u(r; dir_s))))

@@ -33,6 +33,28 @@ __device__ __forceinline__ unsigned long long fix_bits(float v) {
 }
 #endif
 
+// The z-row stride (words) of a spreading brick's int32 accumulator: at least n,
+// and, when at most 6 words of padding achieve it, such that the 5 x 5 (y, z)
+// patch of a stencil that a warp adds with one instruction falls in 25 different
+// shared-memory banks (b p + c, b, c < 5, distinct modulo 32); otherwise n.
+__host__ __device__ inline int spread_row_stride(int n) {
+    for (int p = n; p <= n + 6; p++) {
+        unsigned used = 0u;
+        bool ok = true;
+        for (int b = 0; b < 5 && ok; b++)
+            for (int c = 0; c < 5; c++) {
+                const unsigned bit = 1u << ((b * p + c) & 31);
+                if (used & bit) {
+                    ok = false;
+                    break;
+                }
+                used |= bit;
+            }
+        if (ok) return p;
+    }
+    return n;
+}
+
 // Row kinds of the pair-tile lists.
 enum RowKind { ROW_STATE1 = 0, ROW_STATE2 = 1, ROW_DIFF1 = 2, ROW_DIFF2 = 3 };
 
@@ -197,6 +219,8 @@ struct Args {
     const double* displ_in;   // 3*n_in
     const int* slot_of;       // n_in
     double* f_out;            // 3*n_in (ATM force)
+    double* const* io;        // device cell: io[0] unused, io[1] a page-locked host buffer that
+                              // receives the ATM forces in place of f_out (null: f_out)
     double* f_nb;             // 3*n_in (state-1 nonbonded force) or null
     // slot arrays
     const int* orig;          // NA: user index within the replica, -1 for padding

@@ -165,6 +165,32 @@ def test_rbfe_two_ligands_60000(diff):
     check_case(S.rbfe_pme_60000(), diff)
 
 
+def test_page_locked_buffers_give_the_same_results():
+    """Page-locked positions are read without a staging copy and page-locked
+    force buffers are written by the output kernel over the host link: the
+    results must be those of ordinary host buffers, bit for bit."""
+    import torch
+
+    cases = [S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=31 + k) for k in range(3)]
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
+    pos = np.concatenate([c.pos for c in cases])
+    E0, F0, r0 = b.evaluate(pos, as_array=True)
+    M0 = b.energyMatrix(beta=0.4)
+    pos_pin = torch.from_numpy(pos).pin_memory().numpy()
+    F_pin = torch.full(pos.shape, float("nan"), dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        E1, F1, r1 = b.evaluate(pos_pin, out=F_pin, as_array=True)
+        assert np.array_equal(F1, F0) and np.array_equal(E1, E0) and np.array_equal(r1, r0)
+        assert np.array_equal(b.energyMatrix(beta=0.4), M0)
+    # and ordinary buffers again afterwards (the page-locked target is not kept)
+    E2, F2, r2 = b.evaluate(pos, as_array=True)
+    assert np.array_equal(F2, F0) and np.array_equal(F_pin, F0)
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        assert abs(r1[k][atm.RES_KEYS.index("pert")] - ref["usc"]) <= U_TOL
+        assert force_rel(F1[b.offsets[k]:b.offsets[k + 1]], ref["forces"]) <= F_TOL
+
+
 def test_mixed_batch_of_eight_uneven_boxes():
     cases = S.mixed_batch_8()
     b = atm.ReplicaBatch([atm.system_from_case(c)[0] for c in cases], 0)
