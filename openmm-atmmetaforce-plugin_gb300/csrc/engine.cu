@@ -214,11 +214,16 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
     CUDA_CHECK(cudaMallocHost(&h_fnb_, sizeof(double) * 3 * (size_t)n_in_));
     CUDA_CHECK(cudaMallocHost(&h_results_, sizeof(double) * NUM_RES * (size_t)R_));
     CUDA_CHECK(cudaMallocHost(&h_matrix_, sizeof(double) * (size_t)R_ * R_));
-    CUDA_CHECK(cudaMallocHost(&h_reps_, sizeof(RepDev) * (size_t)R_));
-    CUDA_CHECK(cudaMallocHost(&h_beta_, sizeof(double)));
-    CUDA_CHECK(cudaMallocHost(&h_ctl_, 2 * sizeof(int)));
-    CUDA_CHECK(cudaMallocHost(&h_io_, 2 * sizeof(double*)));
-    h_io_[0] = h_io_[1] = nullptr;
+    // parameter block: ctl (2 ints) at 0, io (3 pointers) at 8, beta at 32, the
+    // replica table at kParamReps
+    param_bytes_ = kParamReps + sizeof(RepDev) * (size_t)R_;
+    CUDA_CHECK(cudaMallocHost(&h_params_, param_bytes_));
+    std::memset(h_params_, 0, param_bytes_);
+    h_ctl_ = reinterpret_cast<int*>(h_params_);
+    h_io_ = reinterpret_cast<double**>(h_params_ + 8);
+    h_beta_ = reinterpret_cast<double*>(h_params_ + 32);
+    h_reps_ = reinterpret_cast<RepDev*>(h_params_ + kParamReps);
+    h_io_[0] = h_io_[1] = h_io_[2] = nullptr;
     CUDA_CHECK(cudaMalloc(&d_counts_, 2 * sizeof(long long)));
     CUDA_CHECK(cudaMemset(d_counts_, 0, 2 * sizeof(long long)));
     h_ctl_[0] = 1;
@@ -247,10 +252,7 @@ Engine::~Engine() {
     cudaFreeHost(h_fnb_);
     cudaFreeHost(h_results_);
     cudaFreeHost(h_matrix_);
-    cudaFreeHost(h_reps_);
-    cudaFreeHost(h_beta_);
-    cudaFreeHost(h_ctl_);
-    cudaFreeHost(h_io_);
+    cudaFreeHost(h_params_);
     if (d_counts_) cudaFree(d_counts_);
     cudaFreeHost(h_status_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
@@ -1033,7 +1035,9 @@ void Engine::alloc_device() {
     a.crf = (float)crf_;
     a.alphad = alpha_;
     a.cutoffd = cutoff_;
-    a.reps = dalloc<RepDev>(d_allocs_, R_);
+    d_params_ = dalloc<char>(d_allocs_, param_bytes_);
+    CUDA_CHECK(cudaMemset(d_params_, 0, param_bytes_));
+    a.reps = reinterpret_cast<RepDev*>(d_params_ + kParamReps);
     a.pos_in = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
     {
         std::vector<double> d(3 * (size_t)n_in_);
@@ -1043,11 +1047,7 @@ void Engine::alloc_device() {
     }
     a.slot_of = dupload(d_allocs_, slot_of_);
     a.f_out = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
-    {
-        double** io = dalloc<double*>(d_allocs_, 2);
-        CUDA_CHECK(cudaMemset(io, 0, 2 * sizeof(double*)));
-        a.io = io;
-    }
+    a.io = reinterpret_cast<double**>(d_params_ + 8);
     a.f_nb = dalloc<double>(d_allocs_, 3 * (size_t)n_in_);
     a.orig = dupload(d_allocs_, orig_);
     a.qs = dupload(d_allocs_, qs_);
@@ -1058,11 +1058,7 @@ void Engine::alloc_device() {
     a.posq_ref = dalloc<float4>(d_allocs_, NA_);
     a.rep_hmax = dalloc<unsigned>(d_allocs_, R_);
     a.list_counts = d_counts_;
-    {
-        int* ctl = dalloc<int>(d_allocs_, 2);
-        CUDA_CHECK(cudaMemset(ctl, 0, 2 * sizeof(int)));
-        a.list_ctl = ctl;
-    }
+    a.list_ctl = reinterpret_cast<int*>(d_params_);
     force_build_ = true;  // new buffers hold no lists
     a.block_rep = dupload(d_allocs_, block_rep_);
     a.block_cls = dupload(d_allocs_, block_cls_);
@@ -1152,7 +1148,7 @@ void Engine::alloc_device() {
     }
     a.results = dalloc<double>(d_allocs_, (size_t)R_ * NUM_RES);
     a.matrix = dalloc<double>(d_allocs_, (size_t)R_ * R_);
-    a.beta = dalloc<double>(d_allocs_, 1);
+    a.beta = reinterpret_cast<double*>(d_params_ + 32);
     CUDA_CHECK(cudaMemset(a.status, 0, sizeof(Status)));
 }
 
@@ -1202,10 +1198,7 @@ void Engine::record(cudaStream_t st, int mode) {
         CUDA_CHECK(cudaMemcpyAsync((void*)a.pos_in, h_pos_, sizeof(double) * 3 * (size_t)n_in_,
                                    cudaMemcpyHostToDevice, st));
     }
-    CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
-    CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_CHECK(cudaMemcpyAsync((void*)a.io, h_io_, 2 * sizeof(double*), cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemcpyAsync(d_params_, h_params_, param_bytes_, cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
     launch_prepare(a, st);
     launch_decide(a, st);
@@ -1308,7 +1301,8 @@ bool Engine::check_status_and_grow() {
     return true;
 }
 
-void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned) {
+void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned,
+                 bool host_results) {
     CUDA_CHECK(cudaSetDevice(dev_));
     if (!layout_ready_) {
         build_layout();
@@ -1322,7 +1316,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
         h_ctl_[0] = (force_build_ || skin_ <= 0.0) ? 1 : 0;
         force_build_ = false;
         cudaStream_t st = user ? user : s_main_;
-        if (d_pos)
+        if (d_pos && d_pos != h_io_[0])  // (positions the graph reads in place need no copy)
             CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
                                        cudaMemcpyDeviceToDevice, st));
         if (h_pos_pinned)
@@ -1343,10 +1337,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             if (host_io)
                 CUDA_CHECK(cudaMemcpyAsync((void*)a.pos_in, h_pos_, sizeof(double) * 3 * (size_t)n_in_,
                                            cudaMemcpyHostToDevice, st));
-            CUDA_CHECK(cudaMemcpyAsync(a.reps, h_reps_, sizeof(RepDev) * (size_t)R_, cudaMemcpyHostToDevice, st));
-            CUDA_CHECK(cudaMemcpyAsync((void*)a.beta, h_beta_, sizeof(double), cudaMemcpyHostToDevice, st));
-            CUDA_CHECK(cudaMemcpyAsync((void*)a.list_ctl, h_ctl_, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
-            CUDA_CHECK(cudaMemcpyAsync((void*)a.io, h_io_, 2 * sizeof(double*), cudaMemcpyHostToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync(d_params_, h_params_, param_bytes_, cudaMemcpyHostToDevice, st));
             CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
             mark("start");
             launch_prepare(a, st);
@@ -1396,7 +1387,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             for (auto e : ev) cudaEventDestroy(e);
             times_.erase(times_.begin());
         } else {
-            const int mode = host_io ? 1 : (h_pos_pinned ? 2 : 0);
+            const int mode = host_io ? 1 : ((h_pos_pinned || host_results) ? 2 : 0);
             cudaGraphExec_t& gx = mode == 1 ? graph_host_ : (mode == 2 ? graph_res_ : graph_dev_);
             if (!gx) {
                 cudaGraph_t g;
@@ -1542,9 +1533,16 @@ void Engine::launch_device(const double* d_pos, cudaStream_t stream) {
     update_influence(stream);
     // the control word stays as the last synchronous evaluation left it: 0 with a
     // skin (the device decides), 1 without one (every evaluation builds)
-    CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
-                               cudaMemcpyDeviceToDevice, stream));
+    if (d_pos != h_io_[0])
+        CUDA_CHECK(cudaMemcpyAsync((void*)A_.pos_in, d_pos, sizeof(double) * 3 * (size_t)n_in_,
+                                   cudaMemcpyDeviceToDevice, stream));
     CUDA_CHECK(cudaGraphLaunch(graph_dev_, stream));
+}
+
+void Engine::set_position_source(const double* d_pos) {
+    CUDA_CHECK(cudaSetDevice(dev_));
+    CUDA_CHECK(cudaDeviceSynchronize());  // no evaluation in flight reads the old one
+    h_io_[0] = const_cast<double*>(d_pos);
 }
 
 bool Engine::poll_overflow() {
@@ -1571,16 +1569,30 @@ void Engine::reorder_from_device(const double* d_pos, cudaStream_t stream) {
 }
 
 void Engine::evaluate_device(const double* d_pos, double* d_forces, double* d_results, cudaStream_t stream) {
-    run_device(d_pos, stream);
-    if (d_forces)
-        CUDA_CHECK(cudaMemcpyAsync(d_forces, A_.f_out, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToDevice,
-                                   stream));
-    if (d_results)
-        CUDA_CHECK(cudaMemcpyAsync(d_results, A_.results, sizeof(double) * NUM_RES * (size_t)R_,
-                                   cudaMemcpyDeviceToDevice, stream));
-    CUDA_CHECK(cudaMemcpyAsync(h_results_, A_.results, sizeof(double) * NUM_RES * (size_t)R_, cudaMemcpyDeviceToHost,
-                               stream));
-    CUDA_CHECK(cudaStreamSynchronize(stream));
+    // the evaluation reads the caller's positions in place and writes the caller's
+    // forces and result records itself (no copies before or after the graph); the
+    // records and matrix also end in page-locked host memory
+    double* const keep = h_io_[0];
+    h_io_[0] = const_cast<double*>(d_pos);
+    h_io_[1] = d_forces;
+    h_io_[2] = d_results;
+    try {
+        if (!layout_ready_) {
+            // the layout is built from positions: take them to the host once
+            CUDA_CHECK(cudaMemcpyAsync(h_pos_, d_pos, sizeof(double) * 3 * (size_t)n_in_, cudaMemcpyDeviceToHost,
+                                       stream));
+            CUDA_CHECK(cudaStreamSynchronize(stream));
+            build_layout();
+            alloc_device();
+        }
+        run(false, stream, d_pos, nullptr, true);  // synchronises
+    } catch (...) {
+        h_io_[0] = keep;
+        h_io_[1] = h_io_[2] = nullptr;
+        throw;
+    }
+    h_io_[0] = keep;
+    h_io_[1] = h_io_[2] = nullptr;
 }
 
 void Engine::reorder() { layout_ready_ = false; }

@@ -66,6 +66,9 @@ public:
     void set_list_skin(double skin);
     // lists and pair tiles in one persistent kernel (k_find_tiles) or two kernels
     void set_fused(bool fused);
+    // positions read in place by every evaluation from this device buffer (the MD
+    // state), instead of copied into the engine's own; null: copied
+    void set_position_source(const double* d_pos);
     void force_build() { force_build_ = true; }
     double list_skin() const { return skin_; }
     // evaluations run and how many of them built the lists (synchronises the device)
@@ -151,7 +154,10 @@ private:
     // after it)
     void record(cudaStream_t main, int mode);
     void pme_transforms(cudaStream_t st, const std::function<void(const char*)>& mark = nullptr);
-    void run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned = nullptr);
+    // host_results: the result records and matrix end in h_results_ / h_matrix_ (graph
+    // flavour 2) without host positions
+    void run(bool host_io, cudaStream_t user, const double* d_pos, const double* h_pos_pinned = nullptr,
+             bool host_results = false);
     bool check_status_and_grow();
     void destroy_graphs();
 
@@ -227,11 +233,18 @@ private:
     double* h_fnb_ = nullptr;      // 3*n_in
     double* h_results_ = nullptr;  // R*NUM_RES
     double* h_matrix_ = nullptr;   // R*R
+    // The per-evaluation parameters in one page-locked block (list control word,
+    // caller buffers, beta, replica table), which every evaluation copies to its
+    // device mirror with one transfer; the four pointers below point into it.
+    static constexpr size_t kParamReps = 64;  // byte offset of the replica table
+    size_t param_bytes_ = 0;
+    char* h_params_ = nullptr;
+    char* d_params_ = nullptr;
     RepDev* h_reps_ = nullptr;     // R
     double* h_beta_ = nullptr;
     int* h_ctl_ = nullptr;         // list control word, copied to the device by every evaluation
-    double** h_io_ = nullptr;      // [1]: page-locked caller buffer for the forces (null: f_out),
-                                   // copied to the device by every evaluation
+    double** h_io_ = nullptr;      // caller buffers of the next evaluations (Args::io), copied to the
+                                   // device by every evaluation: positions, forces, result records
     Status* h_status_ = nullptr;
 
     // device buffers

@@ -72,7 +72,7 @@ __global__ void k_prepare(Args a) {
     int o = a.orig[s];
     const int nreal = __popc(__ballot_sync(FULL_MASK, o >= 0));  // padding sits at the end of a block
     if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
-    const double* p = a.pos_in + 3 * (size_t)(R.in_off + o);
+    const double* p = (a.io[0] ? a.io[0] : a.pos_in) + 3 * (size_t)(R.in_off + o);
     double xd = p[0], yd = p[1], zd = p[2];
     wrap3d(xd, yd, zd, R);  // FP64 wrap into the unit cell
     float x = (float)xd, y = (float)yd, z = (float)zd;
@@ -249,8 +249,9 @@ __global__ void __launch_bounds__(256) k_exceptions(Args a) {
         int4 ij = a.exc_ij[e];
         ExcParam p = a.exc_p[e];
         const RepDev& R = a.reps[ij.z];
-        const double* xi = a.pos_in + 3 * (size_t)ij.x;
-        const double* xj = a.pos_in + 3 * (size_t)ij.y;
+        const double* pos = a.io[0] ? a.io[0] : a.pos_in;
+        const double* xi = pos + 3 * (size_t)ij.x;
+        const double* xj = pos + 3 * (size_t)ij.y;
         int si = a.slot_of[ij.x], sj = a.slot_of[ij.y];
         if (!ij.w) {
             float g[3];
@@ -1003,6 +1004,8 @@ __global__ void __launch_bounds__(256) k_finalize(Args a) {
         out[RES_E1] = E1;  // the NonbondedForce energy at x and at x + d
         out[RES_E2] = E2;
         out[RES_STATUS] = (double)a.status->overflow;
+        if (a.io[2])
+            for (int k = 0; k < NUM_RES; k++) a.io[2][(size_t)r * NUM_RES + k] = out[k];
     }
 }
 

@@ -219,8 +219,11 @@ struct Args {
     const double* displ_in;   // 3*n_in
     const int* slot_of;       // n_in
     double* f_out;            // 3*n_in (ATM force)
-    double* const* io;        // device cell: io[0] unused, io[1] a page-locked host buffer that
-                              // receives the ATM forces in place of f_out (null: f_out)
+    double* const* io;        // device cells, copied from the host by every evaluation: io[0] the
+                              // caller's device positions, read in place of pos_in; io[1] the
+                              // caller's force buffer (device, or page-locked host memory
+                              // written over the host link) in place of f_out; io[2] the
+                              // caller's device result records (a copy of results); null: unused
     double* f_nb;             // 3*n_in (state-1 nonbonded force) or null
     // slot arrays
     const int* orig;          // NA: user index within the replica, -1 for padding

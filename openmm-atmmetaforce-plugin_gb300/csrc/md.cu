@@ -706,6 +706,7 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
     for (auto v : {&bond_rep, &ang_rep, &pos_rep, &cent_rep}) term_rep_.insert(term_rep_.end(), v->begin(), v->end());
 
     x_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
+    eng_->set_position_source(x_);  // every evaluation reads the MD positions in place
     v_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
     xn_ = md_alloc<double>(allocs_, 3 * (size_t)n_);
     MD_CHECK(cudaMemset(v_, 0, sizeof(double) * 3 * (size_t)n_));
