@@ -650,11 +650,14 @@ __device__ __forceinline__ float rcp_ftz(float x) {
 constexpr float kLog2e = 1.4426950408889634f;
 
 // erfc(x) for x >= 0: Abramowitz & Stegun, Handbook of Mathematical Functions,
-// eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term.
+// eq. 7.1.26 (|error| <= 1.5e-7), sharing exp(-x^2) with the force term:
+// erfc(x) = t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-x^2), t = 1 / (1 + p x).
+constexpr float kErfcP = 0.3275911f;
+constexpr float kErfcA1 = 0.254829592f, kErfcA2 = -0.284496736f, kErfcA3 = 1.421413741f,
+                kErfcA4 = -1.453152027f, kErfcA5 = 1.061405429f;
 __device__ __forceinline__ float erfc_as(float x, float expmx2) {
-    const float t = rcp_ftz(1.0f + 0.3275911f * x);
-    const float p =
-        t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
+    const float t = rcp_ftz(1.0f + kErfcP * x);
+    const float p = t * (kErfcA1 + t * (kErfcA2 + t * (kErfcA3 + t * (kErfcA4 + t * kErfcA5))));
     return p * expmx2;
 }
 
@@ -778,11 +781,17 @@ constexpr int kPackedWords = 3;
 
 // Lane l of a half (its j-slot data pj, lj) writes its slot into the two entries
 // that carry it (entries l & 7 and (l & 7) + 8, component l >= 8).
+// The PME variant stores the j charge times the erfc polynomial's leading
+// coefficient (kPackedChargeScale), which its monic polynomial leaves out.
+template <int METHOD>
+constexpr float kPackedChargeScale = METHOD == 4 ? kErfcA5 : 1.0f;
+
+template <int METHOD>
 __device__ __forceinline__ void store_packed_j(float4* se, int l, float4 pj, float2 lj) {
     const int c = l >> 3;
     float* e0 = reinterpret_cast<float*>(se + kPackedWords * (l & 7));
     float* e1 = reinterpret_cast<float*>(se + kPackedWords * ((l & 7) + 8));
-    const float v[6] = {pj.x, pj.y, pj.z, pj.w, lj.x, lj.y};
+    const float v[6] = {pj.x, pj.y, pj.z, pj.w * kPackedChargeScale<METHOD>, lj.x, lj.y};
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         e0[2 * q + c] = v[q];
@@ -826,26 +835,34 @@ __device__ __forceinline__ void tile_steps_x2(const float4* __restrict__ se, flo
         const f2x qq = f2_mul(pq, w1.y), sig = f2_add(ps, w2.x), eps4 = f2_mul(pe, w2.y);
         f2x e, fr;
         if (METHOD == 4) {
-            // a pair not counted is evaluated at r^2 = 1e30 nm^2, where every term is exactly zero
+            // a pair not counted is evaluated at r^2 = 1e30 nm^2, where every term is
+            // exactly zero.  Written for few constant pairs (each costs two registers
+            // in a loop budgeted at 64): t = 1 / (1 + c alpha r) as (1/r) / (1/r + c alpha),
+            // the erfc polynomial monic (its leading coefficient a5 is carried by the
+            // j charges of the packed layout, kPackedChargeScale), the LJ force as
+            // 6 (E_lj + eps4 s^12).
             const f2x r2s = f2_pack(ia ? ra : 1.0e30f, ib ? rb : 1.0e30f);
             const f2x invr = f2_pack(rsqrt_ftz(f2_lo(r2s)), rsqrt_ftz(f2_hi(r2s)));
             const f2x invr2 = f2_mul(invr, invr);
             const f2x s2 = f2_mul(f2_mul(sig, sig), invr2);
             const f2x s6 = f2_mul(f2_mul(s2, s2), s2);
             const f2x t6 = f2_mul(eps4, s6);
+            const f2x u6 = f2_mul(t6, s6);
+            const f2x elj = f2_sub(u6, t6);
+            const f2x flj = f2_add(u6, elj);  // (F_lj r^2) / 6
             const f2x xa = f2_mul(r2s, f2_splat(-alpha * alpha * kLog2e));
             const f2x ex = f2_pack(ex2_ftz(f2_lo(xa)), ex2_ftz(f2_hi(xa)));
-            const f2x den = f2_fma(f2_splat(0.3275911f * alpha), f2_mul(r2s, invr), f2_splat(1.0f));
-            const f2x t = f2_pack(rcp_ftz(f2_lo(den)), rcp_ftz(f2_hi(den)));
-            f2x p = f2_fma(t, f2_splat(1.061405429f), f2_splat(-1.453152027f));
-            p = f2_fma(t, p, f2_splat(1.421413741f));
-            p = f2_fma(t, p, f2_splat(-0.284496736f));
-            p = f2_fma(t, p, f2_splat(0.254829592f));
-            const f2x ec = f2_mul(f2_mul(f2_mul(t, p), ex), invr);
-            e = f2_fma(qq, ec, f2_fma(t6, s6, f2_sub(0ull, t6)));
-            const f2x lj = f2_fma(s6, f2_splat(12.0f), f2_splat(-6.0f));
-            const f2x cq = f2_mul(qq, f2_fma(f2_splat(1.1283791670955126f * alpha), ex, ec));
-            fr = f2_mul(f2_fma(t6, lj, cq), invr2);
+            const f2x w = f2_add(invr, f2_splat(kErfcP * alpha));
+            const f2x t = f2_mul(f2_pack(rcp_ftz(f2_lo(w)), rcp_ftz(f2_hi(w))), invr);
+            f2x h = f2_add(t, f2_splat(kErfcA4 / kErfcA5));
+            h = f2_fma(t, h, f2_splat(kErfcA3 / kErfcA5));
+            h = f2_fma(t, h, f2_splat(kErfcA2 / kErfcA5));
+            h = f2_fma(t, h, f2_splat(kErfcA1 / kErfcA5));
+            const f2x bq = f2_mul(qq, ex);                      // a5 qq exp(-alpha^2 r^2)
+            const f2x ec = f2_mul(bq, f2_mul(f2_mul(h, t), invr));  // qq erfc(alpha r) / r
+            e = f2_add(ec, elj);
+            const f2x fc = f2_fma(bq, f2_splat(1.1283791670955126f * alpha / kErfcA5), ec);
+            fr = f2_mul(f2_fma(flj, f2_splat(6.0f), fc), invr2);
         } else {
             // reaction field: terms at r^2 (or 1 when not counted), then zeroed by the weight
             const f2x r2s = f2_pack(ia ? ra : 1.0f, ib ? rb : 1.0f);
@@ -1042,7 +1059,7 @@ __device__ __forceinline__ void tile_pairs(const Args& a, int cur, int cur_end, 
         float4* s_p = S.buf;
         float2* s_l = reinterpret_cast<float2*>(S.buf + 64);
         if (packed) {
-            store_packed_j(S.buf + 48 * hf, l, pj, lj);
+            store_packed_j<METHOD>(S.buf + 48 * hf, l, pj, lj);
         } else {
             s_p[32 * hf + l] = pj;
             s_p[32 * hf + l + kHalf] = pj;
