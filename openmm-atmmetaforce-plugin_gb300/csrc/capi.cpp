@@ -603,6 +603,7 @@ int atm_context_create(atm_system_t sys, int device, const char* properties, atm
     c->eng.reset(new Engine(std::move(v), device, !diff));
     c->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     c->eng->set_fused(prop_bool(props, "FusedTiles", false));
+    c->eng->set_spread_owner(prop_bool(props, "SpreadByOwner", true));
     c->forces.resize(3 * (size_t)c->n);
     c->forces_nb.resize(3 * (size_t)c->n);
     c->results.resize(NUM_RES);
@@ -703,6 +704,7 @@ int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, co
     b->eng.reset(new Engine(std::move(v), device, !diff, adjoint));
     b->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     b->eng->set_fused(prop_bool(props, "FusedTiles", false));
+    b->eng->set_spread_owner(prop_bool(props, "SpreadByOwner", true));
     b->results.resize((size_t)NUM_RES * n_replicas);
     b->matrix.resize((size_t)n_replicas * n_replicas);
     *out = b.release();
@@ -935,6 +937,7 @@ int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const
     std::unique_ptr<atm_md_s> m(new atm_md_s);
     m->md.reset(new MDDriver(v, device, !diff, opt));
     m->md->engine().set_fused(prop_bool(props, "FusedTiles", false));
+    m->md->engine().set_spread_owner(prop_bool(props, "SpreadByOwner", true));
     *out = m.release();
     API_END
 }

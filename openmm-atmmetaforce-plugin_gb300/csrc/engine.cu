@@ -787,7 +787,6 @@ void Engine::build_layout() {
                 rd.fft_plan[a] = fft_plan_stages(rd.K[a], fft_stages_);
             }
         }
-        build_bricks();
         // the hand-written transforms need a grid plane (two buffers) in shared memory
         int smem_max = 0;
         CUDA_CHECK(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
@@ -823,6 +822,7 @@ void Engine::build_layout() {
                 rd.conv_cta_e = (int)conv_cta_rep_.size();
             }
         }
+        build_bricks();
     } else {
         for (int r = 0; r < R_; r++) {
             rep_host_[r].conv_cta_b = rep_host_[r].conv_cta_e = 0;
@@ -838,24 +838,44 @@ void Engine::build_layout() {
     layout_ready_ = true;
 }
 
-// Spreading bricks: at most tune_brick_ grid points per dimension, two grids per replica.
+// Spreading bricks: at most tune_brick_ grid points per dimension, two grids per
+// replica.  Spreading by owner needs the hand-written forward transform (it reads
+// the int32 grids) and grids larger than a brick plus the stencil reach (4 points)
+// in every dimension of every replica, so that a brick's padded accumulator never
+// wraps onto itself.
 void Engine::build_bricks() {
     brick_cta_rep_.clear();
     brick_smem_ = 0;
+    spread_owner_ = spread_owner_pref_ && use_fft_;
     for (int r = 0; r < R_; r++) {
         RepDev& rd = rep_host_[r];
         for (int d = 0; d < 3; d++) {
             rd.nbrick[d] = (rd.K[d] + tune_brick_ - 1) / tune_brick_;
             rd.bsz[d] = (rd.K[d] + rd.nbrick[d] - 1) / rd.nbrick[d];
+            if (rd.K[d] < rd.bsz[d] + kOrder - 1) spread_owner_ = false;
         }
         rd.brick_cta_b = (int)brick_cta_rep_.size();
         int nb = rd.nbrick[0] * rd.nbrick[1] * rd.nbrick[2];
         for (int k = 0; k < 2 * nb; k++) brick_cta_rep_.push_back(r);
-        // int32 accumulator of a brick padded by the stencil reach (4 points) on each
-        // side, z rows at a bank-spreading stride
-        brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + 8) * (rd.bsz[1] + 8) *
-                                                  spread_row_stride(rd.bsz[2] + 8)));
     }
+    // int32 accumulator of a brick padded by the stencil reach (4 points) below it
+    // (by owner) or on each side, z rows at a bank-spreading stride
+    const int span = spread_owner_ ? kOrder - 1 : 2 * (kOrder - 1);
+    for (int r = 0; r < R_; r++) {
+        const RepDev& rd = rep_host_[r];
+        brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + span) * (rd.bsz[1] + span) *
+                                                  spread_row_stride(rd.bsz[2] + span)));
+    }
+}
+
+void Engine::set_spread_owner(bool on) {
+    if (on == spread_owner_pref_) return;
+    spread_owner_pref_ = on;
+    if (layout_ready_ && method_ == NonbondedForce::PME) {
+        build_bricks();
+        alloc_device();
+    }
+    destroy_graphs();
 }
 
 // ---------------------------------------------------------------------------
@@ -1105,6 +1125,7 @@ void Engine::alloc_device() {
     if (method_ == NonbondedForce::PME) {
         a.brick_ctas = (int)brick_cta_rep_.size();
         a.brick_smem = brick_smem_;
+        a.spread_owner = spread_owner_ ? 1 : 0;
         a.brick_cta_rep = dupload(d_allocs_, brick_cta_rep_);
         a.qreal = dalloc<float>(d_allocs_, n_real_);
         a.qcplx = dalloc<float2>(d_allocs_, n_cplx_);

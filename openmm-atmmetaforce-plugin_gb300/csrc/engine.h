@@ -66,6 +66,10 @@ public:
     void set_list_skin(double skin);
     // lists and pair tiles in one persistent kernel (k_find_tiles) or two kernels
     void set_fused(bool fused);
+    // PME spreading by owner brick (each atom spread once, bricks added to int32
+    // grids by atomics; used where the grids allow it) or by every brick a stencil
+    // touches (each brick writes only its own points)
+    void set_spread_owner(bool on);
     // positions read in place by every evaluation from this device buffer (the MD
     // state), instead of copied into the engine's own; null: copied
     void set_position_source(const double* d_pos);
@@ -187,6 +191,8 @@ private:
     int tune_brick_ = 16;          // spreading brick edge (grid points)
     bool tune_pme_stream_ = true;  // PME on its own stream
     bool tune_fused_ = false;      // lists and pair tiles in one persistent kernel
+    bool spread_owner_pref_ = true;  // spreading by owner brick where the grids allow it
+    bool spread_owner_ = false;      // ... and in use (build_bricks)
 
     // host copies of the layout
     std::vector<int> orig_, slot_of_, block_rep_, block_cls_;

@@ -392,7 +392,6 @@ __device__ __forceinline__ void make_stencil(float x, float y, float z, const Re
 constexpr int kBrickThreads = 256;
 constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kBrickPad = kOrder - 1;      // stencil reach below and above a brick
-constexpr float kGridScale = 33554432.0f;  // 2^25 fixed-point units per e
 
 // Does the cyclic range of base indices of a box (fractional centre fc and half
 // width fh along one box vector) meet the cyclic interval [o, o + len) of Z_K?
@@ -410,15 +409,18 @@ __device__ __forceinline__ bool cyc_meet(float fc, float fh, int K, int o, int l
 }
 
 // A block's bounding box (centre c, half extents h, nm) in fractional coordinates:
-// centre p . r_d, half width sum_i h_i |r[i][d]| (r the reciprocal box).
-__device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev& R, const int* o, const int* e) {
+// centre p . r_d, half width sum_i h_i |r[i][d]| (r the reciprocal box).  Can an
+// atom of the block have its stencil base in [o, o + e + reach) along every
+// dimension (reach 4: its stencil touches the brick; 0: the brick owns it)?
+__device__ __forceinline__ bool box_meets_brick(float4 c, float4 h, const RepDev& R, const int* o, const int* e,
+                                                int reach) {
     float f[3];
     frac3(c.x, c.y, c.z, R, f);
     const float w0 = h.x * fabsf(R.recip[0]) + h.y * fabsf(R.recip[1]) + h.z * fabsf(R.recip[3]);
     const float w1 = h.y * fabsf(R.recip[2]) + h.z * fabsf(R.recip[4]);
     const float w2 = h.z * fabsf(R.recip[5]);
-    return cyc_meet(f[0], w0, R.K[0], o[0], e[0] + kOrder - 1) && cyc_meet(f[1], w1, R.K[1], o[1], e[1] + kOrder - 1) &&
-           cyc_meet(f[2], w2, R.K[2], o[2], e[2] + kOrder - 1);
+    return cyc_meet(f[0], w0, R.K[0], o[0], e[0] + reach) && cyc_meet(f[1], w1, R.K[1], o[1], e[1] + reach) &&
+           cyc_meet(f[2], w2, R.K[2], o[2], e[2] + reach);
 }
 
 constexpr int kSpreadChunk = kBrickThreads;  // blocks examined per pass (one per thread)
@@ -439,9 +441,11 @@ __device__ __forceinline__ int brick_local(int base, int k, int o, int e, int K)
 
 // Adds the stencils of the atoms of candidate blocks s_cand[0 .. nc) to the brick
 // accumulator: warp w takes candidates w, w + 8, ...; lanes = the block's atoms.
+// An atom is added when its stencil base lies in [o, o + e + reach) (reach 4: its
+// stencil touches the brick; 0: the brick owns it).
 __device__ __forceinline__ void spread_candidates(const Args& a, const RepDev& R, const int* s_cand, int nc, int warp,
                                                   int lane, const int* o, const int* e, int pad, bool padded, int P1,
-                                                  int P2, int* acc, float* st, int b0, int c0) {
+                                                  int P2, int* acc, float* st, int b0, int c0, int reach) {
     for (int ci = warp; ci < nc; ci += kBrickWarps) {
         const int ent = s_cand[ci];
         const int Jc = ent >> 2, code = ent & 3;
@@ -469,7 +473,7 @@ __device__ __forceinline__ void spread_candidates(const Args& a, const RepDev& R
                 if (bs >= R.K[d]) bs -= R.K[d];
                 int v = bs - o[d];
                 v += v < 0 ? R.K[d] : 0;
-                ok = ok && v < e[d] + kOrder - 1;
+                ok = ok && v < e[d] + reach;
                 lb[d] = v + pad;  // local index of the stencil's top point (padded copy)
             }
         }
@@ -541,6 +545,11 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     const int npts = e[0] * e[1] * e[2];
     const size_t G3 = (size_t)R.K[0] * R.K[1] * R.K[2];
     float* G = a.qreal + R.real_off + (size_t)g * G3;
+    // owner mode: the brick spreads the atoms whose stencil base it holds into an
+    // accumulator padded by the stencil reach below it, and adds all of it to the
+    // int32 grid (zeroed before the launch); the grid must exceed a padded brick
+    const bool owner = a.spread_owner != 0;
+    const int reach = owner ? 0 : kOrder - 1;
     // grid 1, the structure-factor update, has only the moving blocks (the last
     // blocks of the replica); a brick none of them reaches is written as zeros
     const bool upd = g == 1;
@@ -550,21 +559,24 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
         for (int J = jbegin + tid; J < R.block_end; J += kBrickThreads) {
             const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
             const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
-            any = any || box_meets_brick(c1, h1, R, o, e) || box_meets_brick(c2, h1, R, o, e);
+            any = any || box_meets_brick(c1, h1, R, o, e, reach) || box_meets_brick(c2, h1, R, o, e, reach);
         }
         if (!__syncthreads_or(any)) {
-            for (int k = tid; k < npts; k += kBrickThreads) {
-                const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
-                G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = 0.0f;
-            }
+            if (!owner)
+                for (int k = tid; k < npts; k += kBrickThreads) {
+                    const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
+                    G[((size_t)(o[0] + lx) * R.K[1] + (o[1] + ly)) * R.K[2] + o[2] + lz] = 0.0f;
+                }
             return;
         }
     }
     // padded copy when the grid is larger than a padded brick in every dimension
-    const bool padded = R.K[0] >= e[0] + 2 * kBrickPad && R.K[1] >= e[1] + 2 * kBrickPad &&
-                        R.K[2] >= e[2] + 2 * kBrickPad;
+    // (owner mode: padded below only, and always)
+    const bool padded = owner || (R.K[0] >= e[0] + 2 * kBrickPad && R.K[1] >= e[1] + 2 * kBrickPad &&
+                                  R.K[2] >= e[2] + 2 * kBrickPad);
     const int pad = padded ? kBrickPad : 0;
-    const int P0 = e[0] + 2 * pad, P1 = e[1] + 2 * pad, P2 = spread_row_stride(e[2] + 2 * pad);
+    const int span = owner ? pad : 2 * pad;
+    const int P0 = e[0] + span, P1 = e[1] + span, Q2 = e[2] + span, P2 = spread_row_stride(Q2);
     int* acc = s_dyn;
     float* st = (float*)(s_dyn + a.brick_smem / 4) + warp * 32 * kStencilWords;  // this warp's staged stencils
     for (int k = tid; k < P0 * P1 * P2; k += kBrickThreads) acc[k] = 0;
@@ -577,12 +589,12 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
         int ent0 = -1, ent1 = -1;
         if (J < R.block_end) {
             if (g == 0) {
-                if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e)) ent0 = J << 2;
+                if (box_meets_brick(a.bb_c[J], a.bb_h[J], R, o, e, reach)) ent0 = J << 2;
             } else if (a.block_cls[J] != 0) {
                 const float4 c1 = a.bb_c[J], h1 = a.bb_h[J], dd = a.block_d[J];
                 const float4 c2 = make_float4(c1.x + dd.x, c1.y + dd.y, c1.z + dd.z, 0.f);
-                if (box_meets_brick(c1, h1, R, o, e)) ent0 = (J << 2) | 1;
-                if (box_meets_brick(c2, h1, R, o, e)) ent1 = (J << 2) | 3;
+                if (box_meets_brick(c1, h1, R, o, e, reach)) ent0 = (J << 2) | 1;
+                if (box_meets_brick(c2, h1, R, o, e, reach)) ent1 = (J << 2) | 3;
             }
         }
         const unsigned m0 = __ballot_sync(FULL_MASK, ent0 >= 0), m1 = __ballot_sync(FULL_MASK, ent1 >= 0);
@@ -596,7 +608,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
             nc += cq;
         }
         if (ncand + nc > kSpreadCandCap) {  // list full: add what is listed first
-            spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0);
+            spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0, reach);
             __syncthreads();
             ncand = 0;
         }
@@ -610,8 +622,25 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
         __syncthreads();
     }
     // 2. all listed candidates at once (one barrier for the whole brick)
-    spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0);
+    spread_candidates(a, R, s_cand, ncand, warp, lane, o, e, pad, padded, P1, P2, acc, st, b0, c0, reach);
     __syncthreads();
+    if (owner) {
+        // 4. the whole accumulator, the brick's points and the reach below it, added
+        // to the int32 grid (integer sums: exact and order independent)
+        int* Gi = reinterpret_cast<int*>(G);
+        const int plane = P1 * Q2;
+        for (int k = tid; k < P0 * plane; k += kBrickThreads) {
+            const int lx = k / plane, r = k - lx * plane, ly = r / Q2, lz = r - ly * Q2;
+            const int v = acc[(lx * P1 + ly) * P2 + lz];
+            if (v == 0) continue;
+            int gx = o[0] - pad + lx, gy = o[1] - pad + ly, gz = o[2] - pad + lz;
+            gx += gx < 0 ? R.K[0] : 0;
+            gy += gy < 0 ? R.K[1] : 0;
+            gz += gz < 0 ? R.K[2] : 0;
+            atomicAdd(Gi + ((size_t)gx * R.K[1] + gy) * R.K[2] + gz, v);
+        }
+        return;
+    }
     // 4. the brick's own points, each written once
     for (int k = tid; k < npts; k += kBrickThreads) {
         const int lx = k / (e[1] * e[2]), ly = (k / e[2]) % e[1], lz = k % e[2];
@@ -622,6 +651,8 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
 
 void launch_spread(const Args& a, cudaStream_t s) {
     if (a.brick_ctas <= 0) return;
+    // owner mode adds every brick into the grids: they start at zero
+    if (a.spread_owner) cudaMemsetAsync(a.qreal, 0, sizeof(float) * (size_t)a.n_real_total, s);
     const int bytes = spread_smem_bytes(a.brick_smem);
     // opt in to more than 48 KB of dynamic shared memory (per device; this runs
     // when the evaluation graph is recorded, not at every evaluation)

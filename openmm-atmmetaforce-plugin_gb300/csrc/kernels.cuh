@@ -18,6 +18,7 @@ constexpr int kTile = 32;
 constexpr int kHalf = 16;  // pair tiles are half blocks: 16 i atoms x 16 j slots
 constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr int kOrder = 5;  // PME B-spline order (OpenMM's)
+constexpr float kGridScale = 33554432.0f;  // charge grids: 2^25 int32 fixed-point units per e
 
 // round(v * 2^32) as a 64-bit two's-complement integer, from 32-bit conversions
 // only (64-bit conversions issue on the FP64 pipe, which is narrow on this GPU).
@@ -280,6 +281,9 @@ struct Args {
     // PME
     int brick_ctas;           // spreading CTAs (all replicas)
     int brick_smem;           // dynamic shared memory of a spreading CTA (bytes)
+    int spread_owner;         // 1: every atom spread once, by the brick of its stencil base, and
+                              // the bricks' accumulators added to the int32 charge grids (zeroed
+                              // first) by integer atomics; the forward transform reads int32
     const int* brick_cta_rep; // replica of each spreading CTA
     float* qreal;             // real grids (charge, then potential)
     float2* qcplx;            // spectra

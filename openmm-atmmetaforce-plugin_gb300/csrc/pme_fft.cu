@@ -324,12 +324,18 @@ __global__ void __launch_bounds__(kFftThreads, 5) k_fft_zy(Args a) {
     }
     cp_async_wait_all();
     __syncthreads();
-    // rows 2p and 2p + 1 as the real and imaginary parts of row p
+    // rows 2p and 2p + 1 as the real and imaginary parts of row p (charge grids
+    // spread by owner hold int32 fixed point)
     const FastDiv fz(K2);
+    const bool fixed = a.spread_owner != 0;
     for (int w = threadIdx.x; w < P * K2; w += blockDim.x) {
         const int p = (int)fz.div((unsigned)w), z = w - p * K2;
-        const float re = raw[(2 * p) * K2 + z];
-        const float im = 2 * p + 1 < K1 ? raw[(2 * p + 1) * K2 + z] : 0.f;
+        float re = raw[(2 * p) * K2 + z];
+        float im = 2 * p + 1 < K1 ? raw[(2 * p + 1) * K2 + z] : 0.f;
+        if (fixed) {
+            re = (float)__float_as_int(re) * (1.0f / kGridScale);
+            im = (float)__float_as_int(im) * (1.0f / kGridScale);
+        }
         b0[p * zs + z] = make_float2(re, im);
     }
     __syncthreads();

@@ -213,6 +213,34 @@ def test_deterministic_bitwise():
     assert a.getPotentialEnergy() == b.getPotentialEnergy()
 
 
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_spreading_by_owner_gives_the_same_bits(diff):
+    """PME spreading by owner brick (each atom spread once, by the brick holding
+    its stencil base; bricks summed into int32 grids by atomics) adds the same
+    integer stencil contributions to every grid point as spreading by every brick
+    a stencil touches, so grids and results must be the same bits.  Grids of
+    several sizes, a triclinic box, and both grids of the difference path (the
+    moving atoms' update grid is mostly empty bricks)."""
+    cases = [S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=41),
+             S.water_ligand_box(9000, 4.5, [24], [(1.6, -1.5, 1.4)], S.PME, 0.9, seed=42),
+             S.triclinic_water_ligand_box(5500, (4.0, 3.8, 3.7), (1.2, -1.0, 0.9), [16], [(1.6, 1.5, 1.4)], S.PME,
+                                          0.9, seed=43)]
+    systems = [atm.system_from_case(c)[0] for c in cases]
+    pos = np.concatenate([c.pos for c in cases])
+    out = {}
+    for owner in (0, 1):
+        b = atm.ReplicaBatch(systems, 0, {"DifferencePath": diff, "SpreadByOwner": owner})
+        out[owner] = b.evaluate(pos, as_array=True), b.energyMatrix(beta=0.4), b.offsets
+    (E0, F0, r0), M0, _ = out[0]
+    (E1, F1, r1), M1, offs = out[1]
+    assert np.array_equal(F0, F1) and np.array_equal(E0, E1) and np.array_equal(r0, r1)
+    assert np.array_equal(M0, M1)
+    for k, c in enumerate(cases):
+        ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+        assert abs(r1[k][atm.RES_KEYS.index("pert")] - ref["usc"]) <= U_TOL, k
+        assert force_rel(F1[offs[k]:offs[k + 1]], ref["forces"]) <= F_TOL, k
+
+
 def test_batch_mixed_sizes_vs_oracle_and_matrix():
     cases = [S.abfe_pme_small(1500, 8, 21), S.abfe_pme_small(4000, 18, 22),
              S.abfe_pme_small(2500, 12, 23, displ=1.2), S.abfe_pme_small(6000, 30, 24)]
