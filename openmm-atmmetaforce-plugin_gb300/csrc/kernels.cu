@@ -375,20 +375,26 @@ __device__ __forceinline__ void make_stencil(float x, float y, float z, const Re
     }
 }
 
-// Charge spreading by bricks.  One CTA owns one brick (at most 16^3 points) of
-// one of a replica's two charge grids.  It lists the atoms whose 5x5x5 stencils
-// reach the brick (block bounding boxes in grid units first, one point of
-// margin for rounding) and adds every stencil into an int32 fixed-point copy of
-// the brick padded by 4 points on each side (2^25 units per e: integer sums are
+// Charge spreading by bricks.  One CTA holds one brick (the tuned edge, 12 to 20
+// points) of one of a replica's two charge grids and adds stencils into an int32
+// fixed-point accumulator in shared memory (2^25 units per e: integer sums are
 // exact and order independent, so the grid is bit-reproducible), one atom per
-// warp at a time with the lanes on its 5x5 (y, z) offsets.  With the padding no
-// stencil point needs a bounds test; the padding belongs to the neighbouring
-// bricks, which add the same atoms themselves, and only the brick's own points
-// are written, each once.  Grids smaller than a padded brick use the same copy
-// unpadded, with per-point tests.  Grid 0: state 1.  Grid 1: the structure-
-// factor update of the moving atoms, -q at x and +q at x + d, in both modes
-// (state 2's grid is Q1 + dQ exactly: the non-moving atoms sit at the same grid
-// points in both states and the integer sums are exact).
+// warp at a time with the lanes on its 5x5 (y, z) offsets; candidate atoms come
+// from block bounding boxes in grid units (one point of margin for rounding).
+//   By owner (spread_owner, the default where the grids allow it): the brick
+//   takes the atoms whose stencil base it holds, each atom is spread once, into an
+//   accumulator padded by the 4-point stencil reach below the brick, and the whole
+//   accumulator is added to the grid (zeroed before) by integer atomics, the reach
+//   landing in the neighbouring bricks' points.
+//   By every touching brick: the brick takes every atom whose stencil reaches it,
+//   padded by 4 points on each side, and writes only its own points, each once;
+//   the padding belongs to the neighbouring bricks, which add the same atoms
+//   themselves.  Grids smaller than a padded brick use the copy unpadded, with
+//   per-point tests.
+// Both sum the same integer contributions into each point.  Grid 0: state 1.
+// Grid 1: the structure-factor update of the moving atoms, -q at x and +q at
+// x + d, in both modes (state 2's grid is Q1 + dQ exactly: the non-moving atoms
+// sit at the same grid points in both states and the integer sums are exact).
 constexpr int kBrickThreads = 256;
 constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kBrickPad = kOrder - 1;      // stencil reach below and above a brick
