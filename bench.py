@@ -29,14 +29,14 @@ METRIC = "ATM evals/sec/replica at 23.5k-atom PME: batched vs plain on one GB300
 F_PAIR = 55.0  # FP32 flops per pair (accounting constant)
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) of one k_tiles launch on this workload, from a
-# one-launch ncu --set full capture of the pair-tile kernel at commit 671f792
-# (92.49 MB read + 5.29 MB write; profiles/k_tiles_abfe-pme-23558x22.md)
-TILES_TRAFFIC_BYTES = 97.78e6
-TILES_CAPTURE = "671f792"
+# one-launch ncu --set full capture of the pair-tile kernel at commit 55d5dbd
+# (92.50 MB read + 6.94 MB write; profiles/k_tiles_abfe-pme-23558x22.md)
+TILES_TRAFFIC_BYTES = 99.43e6
+TILES_CAPTURE = "55d5dbd"
 # warp instructions of one k_tiles launch on this workload (same capture): the
 # kernel is bound by instruction issue, so its issue rate is the second roofline
 # reported
-TILES_WARP_INSTR = 346.1e6
+TILES_WARP_INSTR = 346.5e6
 
 
 def parse():
