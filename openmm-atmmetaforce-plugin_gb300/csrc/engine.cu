@@ -1109,7 +1109,16 @@ void Engine::alloc_device() {
     a.tiles = dalloc<int4>(d_allocs_, tile_cap_);
     a.tile_j = dalloc<int>(d_allocs_, (size_t)kHalf * tile_cap_);
     a.e_tile = dalloc<float2>(d_allocs_, (size_t)nrows_ * row_cap_);
-    a.e_row = dalloc<double>(d_allocs_, (size_t)nrows_);
+    {
+        // finalize: about 32 rows per CTA, at most 64 CTAs per replica
+        int rows = 1;
+        for (int r = 0; r < R_; r++)
+            rows = std::max(rows, (rep_host_[r].row1_e - rep_host_[r].row1_b) + (rep_host_[r].row2_e - rep_host_[r].row2_b));
+        a.fin_ctas = std::min(64, std::max(1, (rows + 31) / 32));
+        a.fin_part = dalloc<unsigned long long>(d_allocs_, (size_t)R_ * a.fin_ctas * 2);
+        a.fin_count = dalloc<int>(d_allocs_, (size_t)R_);
+        CUDA_CHECK(cudaMemset(a.fin_count, 0, sizeof(int) * (size_t)R_));
+    }
     a.status = dalloc<Status>(d_allocs_, 1);
     a.F = dalloc<unsigned long long>(d_allocs_, 6 * (size_t)NA_);
     a.adjoint = adjoint_ ? 1 : 0;

@@ -975,58 +975,100 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
     out[RES_DWDU] = (alpha > 0 ? bfp : l2) * fp;
 }
 
-// Energy of each tile row, one warp per row (lanes over the row's slots, fixed order).
-__global__ void k_rowsum(Args a) {
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (row >= a.nrows) return;
-    const int n = a.row_count[row];
-    const float2* e = a.e_tile + (size_t)row * a.row_cap;
-    double s = 0.0;
-    for (int k = lane; k < n; k += 32) {
-        const float2 v = e[k];
-        s += (double)v.x + (double)v.y;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
-    if (lane == 0) a.e_row[row] = s;
-}
+// Energies of a replica and the ATM merge, one kernel: CTA c of replica r sums
+// the tile energies of the replica's rows c, c + C, ... (C = fin_ctas; rows of
+// state 1, then rows of state 2 or of the difference tiles), warp per row, lanes
+// over its slots, as int64 fixed point (2^32 per kJ/mol: exact, order
+// independent sums, on the integer pipe rather than the narrow FP64 one), and
+// writes its two partials; the last CTA of the replica to finish (a counter it
+// resets for the next evaluation) adds the partials, the exceptions' and the
+// reciprocal sum's partials (FP64) and runs the FP64 merge.
+constexpr int kFinThreads = 256;
 
-__device__ double rows_sum(const Args& a, int rb, int re) {
-    double s = 0.0;
-    for (int row = rb + threadIdx.x; row < re; row += blockDim.x) s += a.e_row[row];
-    return s;
-}
+__device__ __forceinline__ long long fix_e(float v) { return (long long)fix_bits(v); }
 
-__global__ void __launch_bounds__(256) k_finalize(Args a) {
-    // seven sums per replica in one fixed-order reduction: direct-space rows of
-    // state 1 and state 2 / difference, exceptions (3), reciprocal (2)
-    __shared__ double sh[7][8];
-    const int r = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
+    __shared__ long long sh_i[2][kFinThreads / 32];
+    __shared__ double sh[5][kFinThreads / 32];
+    __shared__ int s_last;
+    const int C = a.fin_ctas;
+    const int r = blockIdx.x / C, c = blockIdx.x - r * C;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const RepDev& R = a.reps[r];
-    double v[7] = {rows_sum(a, R.row1_b, R.row1_e), rows_sum(a, R.row2_b, R.row2_e), 0, 0, 0, 0, 0};
-    for (int c = R.exc_cta_b + threadIdx.x; c < R.exc_cta_e; c += blockDim.x) {
-        v[2] += a.e_part_exc[3 * c];
-        v[3] += a.e_part_exc[3 * c + 1];
-        v[4] += a.e_part_exc[3 * c + 2];
-    }
-    for (int c = R.conv_cta_b + threadIdx.x; c < R.conv_cta_e; c += blockDim.x) {
-        v[5] += a.e_part_conv[2 * c];
-        v[6] += a.e_part_conv[2 * c + 1];
+    const int n1 = R.row1_e - R.row1_b, n2 = R.row2_e - R.row2_b;
+    long long s1 = 0, s2 = 0;
+    for (int k = c + C * w; k < n1 + n2; k += C * (kFinThreads / 32)) {
+        const int row = k < n1 ? R.row1_b + k : R.row2_b + (k - n1);
+        const int n = a.row_count[row];
+        const float2* e = a.e_tile + (size_t)row * a.row_cap;
+        long long t = 0;
+        for (int q = lane; q < n; q += 32) {
+            const float2 v = e[q];
+            t += fix_e(v.x) + fix_e(v.y);
+        }
+        if (k < n1)
+            s1 += t;
+        else
+            s2 += t;
     }
 #pragma unroll
-    for (int k = 0; k < 7; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(FULL_MASK, s1, o);
+        s2 += __shfl_xor_sync(FULL_MASK, s2, o);
+    }
+    if (lane == 0) {
+        sh_i[0][w] = s1;
+        sh_i[1][w] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t1 = 0, t2 = 0;
+        for (int q = 0; q < kFinThreads / 32; q++) {
+            t1 += sh_i[0][q];
+            t2 += sh_i[1][q];
+        }
+        a.fin_part[2 * (size_t)blockIdx.x] = (unsigned long long)t1;
+        a.fin_part[2 * (size_t)blockIdx.x + 1] = (unsigned long long)t2;
+        __threadfence();
+        s_last = atomicAdd(&a.fin_count[r], 1) == C - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // the replica's last CTA: partials of the rows (fixed order), the exceptions
+    // (3) and the reciprocal sum (2)
+    double v[5] = {0, 0, 0, 0, 0};
+    for (int q = R.exc_cta_b + threadIdx.x; q < R.exc_cta_e; q += blockDim.x) {
+        v[0] += a.e_part_exc[3 * q];
+        v[1] += a.e_part_exc[3 * q + 1];
+        v[2] += a.e_part_exc[3 * q + 2];
+    }
+    for (int q = R.conv_cta_b + threadIdx.x; q < R.conv_cta_e; q += blockDim.x) {
+        v[3] += a.e_part_conv[2 * q];
+        v[4] += a.e_part_conv[2 * q + 1];
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], o);
         if (lane == 0) sh[k][w] = v[k];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t[7];
-        for (int k = 0; k < 7; k++) {
-            t[k] = 0.0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); q++) t[k] += sh[k][q];
+        a.fin_count[r] = 0;  // ready for the next evaluation
+        long long d1 = 0, d2 = 0;
+        const volatile unsigned long long* part = a.fin_part + 2 * (size_t)r * C;
+        for (int q = 0; q < C; q++) {
+            d1 += (long long)part[2 * q];
+            d2 += (long long)part[2 * q + 1];
         }
-        const double dir1 = t[0], dir2 = t[1], x1 = t[2], x2 = t[3], xd = t[4], c1 = t[5], c2 = t[6];
+        double t[5];
+        for (int k = 0; k < 5; k++) {
+            t[k] = 0.0;
+            for (int q = 0; q < kFinThreads / 32; q++) t[k] += sh[k][q];
+        }
+        const double dir1 = (double)d1 * (1.0 / 4294967296.0), dir2 = (double)d2 * (1.0 / 4294967296.0);
+        const double x1 = t[0], x2 = t[1], xd = t[2], c1 = t[3], c2 = t[4];
         double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
         double E2;
         if (a.full) {
@@ -1047,8 +1089,7 @@ __global__ void __launch_bounds__(256) k_finalize(Args a) {
 }
 
 void launch_finalize(const Args& a, cudaStream_t s) {
-    k_rowsum<<<(a.nrows * 32 + 255) / 256, 256, 0, s>>>(a);
-    k_finalize<<<a.R, 256, 0, s>>>(a);
+    k_finalize<<<a.R * a.fin_ctas, kFinThreads, 0, s>>>(a);
 }
 
 // Hybrid forces in user order: thread g takes input atom g (its slot from

@@ -262,7 +262,9 @@ struct Args {
     int fused;                // 1: lists and pair tiles in one persistent kernel (k_find_tiles)
     int* tile_j;              // 32 j slots per tile (atom tiles)
     float2* e_tile;           // nrows*row_cap: tile energies as (hi, lo) FP32 pairs, summed in FP64 per row
-    double* e_row;            // nrows: sum of each row's tiles
+    int fin_ctas;             // finalize CTAs per replica (row sums), the last one merges
+    unsigned long long* fin_part;  // R x fin_ctas x 2: int64 fixed-point row-energy partials
+    int* fin_count;           // R: finalize CTAs done (the last resets it to 0)
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]
     unsigned long long* F;
