@@ -1213,8 +1213,9 @@ int Engine::tile_dynamic() const {
 }
 
 int Engine::launches_per_eval() const {
-    // prepare, decide, find, tiles, exceptions, row sums, finalize, output, matrix (+ PME kernels)
-    int n = 4 + 5;  // + the list decision
+    // prepare, decide, find and tiles (or the fused kernel), exceptions, finalize
+    // (with the row sums), output, matrix (+ PME kernels)
+    int n = tune_fused_ ? 7 : 8;
     // spread, gather (moving atoms included) and the transforms: three of ours
     // (zy, x + convolution, inverse yz), or the convolution between library ones
     if (method_ == NonbondedForce::PME) n += use_fft_ ? 5 : 3;
