@@ -108,6 +108,14 @@ static bool prop_bool(const std::map<std::string, std::string>& m, const char* k
     throw Error(ATM_ERR_INVALID_ARGUMENT, std::string("Bad value for property ") + key + ": " + v);
 }
 
+static double prop_double(const std::map<std::string, std::string>& m, const char* key, double def);
+
+// SpreadBrick=n: the PME spreading brick edge in grid points (0: per atom), as the
+// autotuner would choose it; absent: the engine's default until a tuning.
+static void apply_spread_brick(Engine& e, const std::map<std::string, std::string>& m) {
+    if (m.count("SpreadBrick")) e.set_spread_brick((int)prop_double(m, "SpreadBrick", 16.0));
+}
+
 static double prop_double(const std::map<std::string, std::string>& m, const char* key, double def) {
     auto it = m.find(key);
     if (it == m.end()) return def;
@@ -604,6 +612,7 @@ int atm_context_create(atm_system_t sys, int device, const char* properties, atm
     c->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     c->eng->set_fused(prop_bool(props, "FusedTiles", false));
     c->eng->set_spread_owner(prop_bool(props, "SpreadByOwner", true));
+    apply_spread_brick(*c->eng, props);
     c->forces.resize(3 * (size_t)c->n);
     c->forces_nb.resize(3 * (size_t)c->n);
     c->results.resize(NUM_RES);
@@ -705,6 +714,7 @@ int atm_batch_create(const atm_system_t* systems, int n_replicas, int device, co
     b->eng->set_list_skin(prop_double(props, "ListSkin", 0.0));
     b->eng->set_fused(prop_bool(props, "FusedTiles", false));
     b->eng->set_spread_owner(prop_bool(props, "SpreadByOwner", true));
+    apply_spread_brick(*b->eng, props);
     b->results.resize((size_t)NUM_RES * n_replicas);
     b->matrix.resize((size_t)n_replicas * n_replicas);
     *out = b.release();
@@ -938,6 +948,7 @@ int atm_md_create(const atm_system_t* systems, int n_replicas, int device, const
     m->md.reset(new MDDriver(v, device, !diff, opt));
     m->md->engine().set_fused(prop_bool(props, "FusedTiles", false));
     m->md->engine().set_spread_owner(prop_bool(props, "SpreadByOwner", true));
+    apply_spread_brick(m->md->engine(), props);
     *out = m.release();
     API_END
 }

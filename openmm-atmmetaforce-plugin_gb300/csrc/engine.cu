@@ -842,15 +842,18 @@ void Engine::build_layout() {
 // replica.  Spreading by owner needs the hand-written forward transform (it reads
 // the int32 grids) and grids larger than a brick plus the stencil reach (4 points)
 // in every dimension of every replica, so that a brick's padded accumulator never
-// wraps onto itself.
+// wraps onto itself.  tune_brick_ 0: spreading per atom (k_spread_atoms, int32
+// grids, also with the hand-written transform only; bricks of 16 otherwise).
 void Engine::build_bricks() {
     brick_cta_rep_.clear();
     brick_smem_ = 0;
+    spread_atoms_ = tune_brick_ == 0 && use_fft_;
+    const int edge = tune_brick_ > 0 ? tune_brick_ : 16;
     spread_owner_ = spread_owner_pref_ && use_fft_;
     for (int r = 0; r < R_; r++) {
         RepDev& rd = rep_host_[r];
         for (int d = 0; d < 3; d++) {
-            rd.nbrick[d] = (rd.K[d] + tune_brick_ - 1) / tune_brick_;
+            rd.nbrick[d] = (rd.K[d] + edge - 1) / edge;
             rd.bsz[d] = (rd.K[d] + rd.nbrick[d] - 1) / rd.nbrick[d];
             if (rd.K[d] < rd.bsz[d] + kOrder - 1) spread_owner_ = false;
         }
@@ -866,6 +869,11 @@ void Engine::build_bricks() {
         brick_smem_ = std::max(brick_smem_, (int)(sizeof(int) * (rd.bsz[0] + span) * (rd.bsz[1] + span) *
                                                   spread_row_stride(rd.bsz[2] + span)));
     }
+}
+
+void Engine::set_spread_brick(int brick) {
+    if (brick < 0 || (brick > 0 && brick < kOrder)) throw Error(1, "SpreadBrick must be 0 (per atom) or at least 5");
+    apply_tuning(tune_tile_per_sm_ > 0 ? tune_tile_per_sm_ : max_tile_per_sm_, brick, tune_pme_stream_, tune_fused_);
 }
 
 void Engine::set_spread_owner(bool on) {
@@ -956,7 +964,9 @@ std::string Engine::autotune(int trials, bool use_cache) {
     int bt = max_tile_per_sm_, bb = tune_brick_;
     bool bs = tune_pme_stream_, bf = tune_fused_;
     const bool pme = method_ == NonbondedForce::PME;
+    // spreading bricks of 20, 19, 16, 12 points, or per atom (0: small systems)
     std::vector<int> bricks = pme ? std::vector<int>{20, 19, 16, 12} : std::vector<int>{tune_brick_};
+    if (pme && use_fft_) bricks.push_back(0);
     std::vector<int> pmes = pme ? std::vector<int>{1, 0} : std::vector<int>{1};
     cudaEvent_t e0, e1;
     CUDA_CHECK(cudaEventCreate(&e0));
@@ -1134,7 +1144,8 @@ void Engine::alloc_device() {
     if (method_ == NonbondedForce::PME) {
         a.brick_ctas = (int)brick_cta_rep_.size();
         a.brick_smem = brick_smem_;
-        a.spread_owner = spread_owner_ ? 1 : 0;
+        a.spread_owner = spread_owner_ || spread_atoms_ ? 1 : 0;
+        a.spread_atoms = spread_atoms_ ? 1 : 0;
         a.brick_cta_rep = dupload(d_allocs_, brick_cta_rep_);
         a.qreal = dalloc<float>(d_allocs_, n_real_);
         a.qcplx = dalloc<float2>(d_allocs_, n_cplx_);

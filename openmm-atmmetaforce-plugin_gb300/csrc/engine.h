@@ -70,6 +70,9 @@ public:
     // grids by atomics; used where the grids allow it) or by every brick a stencil
     // touches (each brick writes only its own points)
     void set_spread_owner(bool on);
+    // the spreading brick edge (grid points; 0: spreading per atom with atomics into
+    // the grids), as the autotuner would set it
+    void set_spread_brick(int brick);
     // positions read in place by every evaluation from this device buffer (the MD
     // state), instead of copied into the engine's own; null: copied
     void set_position_source(const double* d_pos);
@@ -193,6 +196,7 @@ private:
     bool tune_fused_ = false;      // lists and pair tiles in one persistent kernel
     bool spread_owner_pref_ = true;  // spreading by owner brick where the grids allow it
     bool spread_owner_ = false;      // ... and in use (build_bricks)
+    bool spread_atoms_ = false;      // spreading per atom (tune_brick_ 0, hand-written transform)
 
     // host copies of the layout
     std::vector<int> orig_, slot_of_, block_rep_, block_cls_;

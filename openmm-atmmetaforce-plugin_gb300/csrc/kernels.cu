@@ -655,7 +655,89 @@ __global__ void __launch_bounds__(kBrickThreads) k_spread(Args a) {
     }
 }
 
+// Spreading per atom, for systems too small to fill the GPU with bricks: a warp
+// takes one block of 32 atoms (grid 0: every block at x; grid 1: every moving
+// block at x with -q and at x + d with +q), each lane computes its atom's stencil,
+// then the atoms one by one with the lanes on the 5 x 5 (y, z) offsets add their
+// 125 points to the int32 grid by atomics.  The integer contribution of an atom to
+// a point is computed exactly as the bricks compute it, so the grids are the same
+// bits.
+constexpr int kSpreadAtomWarps = 8;
+
+__global__ void __launch_bounds__(kSpreadAtomWarps * 32) k_spread_atoms(Args a) {
+    __shared__ float s_st[kSpreadAtomWarps][32 * kStencilWords];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * kSpreadAtomWarps + w;
+    if (item >= a.NB + 2 * a.n_mov_blocks) return;
+    int blk, code;  // 0: grid 0 at x; 1: grid 1, -q at x; 3: grid 1, +q at x + d
+    if (item < a.NB) {
+        blk = item;
+        code = 0;
+    } else {
+        const int m = item - a.NB;
+        blk = a.mov_blocks[m >> 1];
+        code = (m & 1) ? 3 : 1;
+    }
+    const RepDev& R = a.reps[a.block_rep[blk]];
+    const int s = blk * kTile + lane;
+    const int nreal = __float_as_int(a.bb_h[blk].w);
+    float4 p = a.posq[s];
+    if (code == 1) p.w = -p.w;
+    if (code == 3) {
+        const float4 dd = a.displ[s];
+        p.x += dd.x;
+        p.y += dd.y;
+        p.z += dd.z;
+        wrap3(p.x, p.y, p.z, R);
+    }
+    const bool ok = lane < nreal && p.w != 0.0f;
+    float* st = s_st[w];
+    if (ok) {
+        Stencil S;
+        make_stencil(p.x, p.y, p.z, R, S, false);
+        float* wv = st + lane * kStencilWords;
+        const float qs = p.w * kGridScale;
+#pragma unroll
+        for (int k = 0; k < kOrder; k++) {
+            wv[k] = qs * S.w[0][k];
+            wv[kOrder + k] = S.w[1][k];
+            wv[2 * kOrder + k] = S.w[2][k];
+        }
+        wv[15] = __int_as_float((S.base[0] << 20) | (S.base[1] << 10) | S.base[2]);
+    }
+    unsigned bal = __ballot_sync(FULL_MASK, ok);
+    __syncwarp();
+    const int K0 = R.K[0], K1 = R.K[1], K2 = R.K[2];
+    int* G = reinterpret_cast<int*>(a.qreal + R.real_off + (code ? (size_t)K0 * K1 * K2 : 0));
+    const int b0 = lane / kOrder, c0 = lane % kOrder;
+    while (bal) {
+        const int src = __ffs(bal) - 1;
+        bal &= bal - 1;
+        const float* wv = st + src * kStencilWords;
+        if (lane < kOrder * kOrder) {
+            const int bases = __float_as_int(wv[15]);
+            int y = ((bases >> 10) & 1023) - b0, z = (bases & 1023) - c0;
+            y += y < 0 ? K1 : 0;
+            z += z < 0 ? K2 : 0;
+            const float wyz = wv[kOrder + b0] * wv[2 * kOrder + c0];
+            const int x0 = bases >> 20;
+#pragma unroll
+            for (int a0 = 0; a0 < kOrder; a0++) {
+                int x = x0 - a0;
+                x += x < 0 ? K0 : 0;
+                atomicAdd(G + ((size_t)x * K1 + y) * K2 + z, __float2int_rn(wv[a0] * wyz));
+            }
+        }
+    }
+}
+
 void launch_spread(const Args& a, cudaStream_t s) {
+    if (a.spread_atoms) {
+        cudaMemsetAsync(a.qreal, 0, sizeof(float) * (size_t)a.n_real_total, s);
+        const int items = a.NB + 2 * a.n_mov_blocks;
+        k_spread_atoms<<<(items + kSpreadAtomWarps - 1) / kSpreadAtomWarps, kSpreadAtomWarps * 32, 0, s>>>(a);
+        return;
+    }
     if (a.brick_ctas <= 0) return;
     // owner mode adds every brick into the grids: they start at zero
     if (a.spread_owner) cudaMemsetAsync(a.qreal, 0, sizeof(float) * (size_t)a.n_real_total, s);

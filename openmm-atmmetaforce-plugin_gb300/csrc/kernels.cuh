@@ -283,9 +283,10 @@ struct Args {
     // PME
     int brick_ctas;           // spreading CTAs (all replicas)
     int brick_smem;           // dynamic shared memory of a spreading CTA (bytes)
-    int spread_owner;         // 1: every atom spread once, by the brick of its stencil base, and
-                              // the bricks' accumulators added to the int32 charge grids (zeroed
-                              // first) by integer atomics; the forward transform reads int32
+    int spread_owner;         // 1: the charge grids are int32, zeroed before the spreading and
+                              // summed by integer atomics (the forward transform reads int32):
+                              // every atom spread once, by the brick of its stencil base, or
+    int spread_atoms;         //   (1) by its own warp straight into the grids (small systems)
     const int* brick_cta_rep; // replica of each spreading CTA
     float* qreal;             // real grids (charge, then potential)
     float2* qcplx;            // spectra

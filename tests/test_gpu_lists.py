@@ -117,6 +117,17 @@ def test_md_with_kept_lists_follows_the_rebuilt_trajectory():
     assert a.listInfo()["builds"] == a.listInfo()["evaluations"]
 
 
+def test_md_spreading_per_atom_follows_the_same_trajectory():
+    """Spreading per atom (SpreadBrick=0) adds the same integer stencil
+    contributions to the charge grids as the bricks: an MD run with it follows the
+    trajectory of bricks of 16 bit for bit."""
+    a = _md({"ListSkin": 0.1, "SpreadBrick": 16}, 30)
+    b = _md({"ListSkin": 0.1, "SpreadBrick": 0}, 30)
+    xa = a.getState(getPositions=True).getPositions()
+    xb = b.getState(getPositions=True).getPositions()
+    assert np.array_equal(xa, xb)
+
+
 def test_md_check_that_reports_an_overflow_redoes_the_steps():
     """The host-side fake makes the second list check report an overflow: the
     state goes back to the snapshot of the first check and the steps run again,

@@ -216,11 +216,12 @@ def test_deterministic_bitwise():
 @pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
 def test_spreading_by_owner_gives_the_same_bits(diff):
     """PME spreading by owner brick (each atom spread once, by the brick holding
-    its stencil base; bricks summed into int32 grids by atomics) adds the same
-    integer stencil contributions to every grid point as spreading by every brick
-    a stencil touches, so grids and results must be the same bits.  Grids of
-    several sizes, a triclinic box, and both grids of the difference path (the
-    moving atoms' update grid is mostly empty bricks)."""
+    its stencil base; bricks summed into int32 grids by atomics) and spreading per
+    atom (SpreadBrick=0: each atom's stencil added straight into the grid by
+    atomics) add the same integer stencil contributions to every grid point as
+    spreading by every brick a stencil touches, so grids and results must be the
+    same bits.  Grids of several sizes, a triclinic box, and both grids of the
+    difference path (the moving atoms' update grid is mostly empty bricks)."""
     cases = [S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=41),
              S.water_ligand_box(9000, 4.5, [24], [(1.6, -1.5, 1.4)], S.PME, 0.9, seed=42),
              S.triclinic_water_ligand_box(5500, (4.0, 3.8, 3.7), (1.2, -1.0, 0.9), [16], [(1.6, 1.5, 1.4)], S.PME,
@@ -228,13 +229,16 @@ def test_spreading_by_owner_gives_the_same_bits(diff):
     systems = [atm.system_from_case(c)[0] for c in cases]
     pos = np.concatenate([c.pos for c in cases])
     out = {}
-    for owner in (0, 1):
-        b = atm.ReplicaBatch(systems, 0, {"DifferencePath": diff, "SpreadByOwner": owner})
-        out[owner] = b.evaluate(pos, as_array=True), b.energyMatrix(beta=0.4), b.offsets
-    (E0, F0, r0), M0, _ = out[0]
-    (E1, F1, r1), M1, offs = out[1]
-    assert np.array_equal(F0, F1) and np.array_equal(E0, E1) and np.array_equal(r0, r1)
-    assert np.array_equal(M0, M1)
+    modes = {"touching bricks": {"SpreadByOwner": 0}, "owner bricks": {"SpreadByOwner": 1},
+             "per atom": {"SpreadBrick": 0}, "owner bricks of 12": {"SpreadBrick": 12}}
+    for name, props in modes.items():
+        b = atm.ReplicaBatch(systems, 0, {"DifferencePath": diff, **props})
+        out[name] = b.evaluate(pos, as_array=True), b.energyMatrix(beta=0.4), b.offsets
+    (E0, F0, r0), M0, _ = out["touching bricks"]
+    for name in modes:
+        (E1, F1, r1), M1, offs = out[name]
+        assert np.array_equal(F0, F1) and np.array_equal(E0, E1) and np.array_equal(r0, r1), name
+        assert np.array_equal(M0, M1), name
     for k, c in enumerate(cases):
         ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
         assert abs(r1[k][atm.RES_KEYS.index("pert")] - ref["usc"]) <= U_TOL, k
