@@ -1224,9 +1224,9 @@ int Engine::tile_dynamic() const {
 }
 
 int Engine::launches_per_eval() const {
-    // prepare (with the list decision), find and tiles (or the fused kernel),
-    // exceptions, finalize (with the row sums), output, matrix (+ PME kernels)
-    int n = tune_fused_ ? 6 : 7;
+    // prepare, decide, find and tiles (or the fused kernel), exceptions, finalize
+    // (with the row sums), output, matrix (+ PME kernels)
+    int n = tune_fused_ ? 7 : 8;
     // spread, gather (moving atoms included) and the transforms: three of ours
     // (zy, x + convolution, inverse yz), or the convolution between library ones
     if (method_ == NonbondedForce::PME) n += use_fft_ ? 5 : 3;
@@ -1243,6 +1243,7 @@ void Engine::record(cudaStream_t st, int mode) {
     CUDA_CHECK(cudaMemcpyAsync(d_params_, h_params_, param_bytes_, cudaMemcpyHostToDevice, st));
     CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
     launch_prepare(a, st);
+    launch_decide(a, st);
     bool pme = method_ == NonbondedForce::PME;
     if (pme) {
         // the PME chain on its own stream (overlapping the pair tiles) or in line,
@@ -1382,6 +1383,7 @@ void Engine::run(bool host_io, cudaStream_t user, const double* d_pos, const dou
             CUDA_CHECK(cudaMemsetAsync(a.rep_hmax, 0, sizeof(unsigned) * (size_t)R_, st));
             mark("start");
             launch_prepare(a, st);
+            launch_decide(a, st);
             mark("prepare");
             if (a.fused) {
                 launch_find_tiles(a, st);

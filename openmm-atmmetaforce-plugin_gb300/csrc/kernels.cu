@@ -62,51 +62,10 @@ __device__ __forceinline__ void warp_bbox(float x, float y, float z, const RepDe
     }
 }
 
-// Whether this evaluation builds the lists: when forced, with no skin, or when an
-// atom has moved more than skin / 2 since the last build (then no pair within the
-// cutoff now was beyond rc + skin then).  A build resets the finder's counters.
-// Run by one thread after every atom's displacement is known.
-__device__ void decide_lists(const Args& a) {
-    Status* st = a.status;
-    const float d2 = __uint_as_float(*reinterpret_cast<volatile unsigned*>(&st->disp2));
-    const bool build = a.list_ctl[0] != 0 || !(a.skin_half2 > 0.f) || d2 > a.skin_half2;
-    st->sticky |= st->overflow;
-    if (build) {
-        st->tile_count = 0;
-        st->overflow = 0;
-        st->max_row = 0;
-    }
-    st->next_row = 0;  // the fused kernel walks the rows at every evaluation
-    st->rebuild = build ? 1 : 0;
-    st->disp2 = 0u;
-    a.list_counts[0]++;
-    if (build) a.list_counts[1]++;
-}
-
-__device__ __forceinline__ void prepare_block(const Args& a, int b, int lane);
-
-// Positions to slots, block boxes, cleared force planes and the skin's
-// displacement test, warp per block; the last CTA to finish (a counter it resets)
-// then decides whether this evaluation builds the lists.
 __global__ void k_prepare(Args a) {
-    const int lane = threadIdx.x & 31;
-    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (b < a.NB) prepare_block(a, b, lane);
-    __shared__ int s_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = atomicAdd(&a.status->prep_done, 1) == (int)gridDim.x - 1;
-    }
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-        __threadfence();
-        a.status->prep_done = 0;
-        decide_lists(a);
-    }
-}
-
-__device__ __forceinline__ void prepare_block(const Args& a, int b, int lane) {
+    int lane = threadIdx.x & 31;
+    int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= a.NB) return;
     int s = b * kTile + lane;
     int rep = a.block_rep[b];
     const RepDev& R = a.reps[rep];
@@ -158,6 +117,28 @@ void launch_prepare(const Args& a, cudaStream_t s) {
     k_prepare<<<blocks, threads, 0, s>>>(a);
 }
 
+// Whether this evaluation builds the lists: when forced, with no skin, or when an
+// atom has moved more than skin / 2 since the last build (then no pair within the
+// cutoff now was beyond rc + skin then).  A build resets the finder's counters.
+__global__ void k_decide(Args a) {
+    if (threadIdx.x != 0) return;
+    Status* st = a.status;
+    const float d2 = __uint_as_float(st->disp2);
+    const bool build = a.list_ctl[0] != 0 || !(a.skin_half2 > 0.f) || d2 > a.skin_half2;
+    st->sticky |= st->overflow;
+    if (build) {
+        st->tile_count = 0;
+        st->overflow = 0;
+        st->max_row = 0;
+    }
+    st->next_row = 0;  // the fused kernel walks the rows at every evaluation
+    st->rebuild = build ? 1 : 0;
+    st->disp2 = 0u;
+    a.list_counts[0]++;
+    if (build) a.list_counts[1]++;
+}
+
+void launch_decide(const Args& a, cudaStream_t s) { k_decide<<<1, 32, 0, s>>>(a); }
 
 // ---------------------------------------------------------------------------
 // find: one warp per row; bounding-box test of block I against candidates J

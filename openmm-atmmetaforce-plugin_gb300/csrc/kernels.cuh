@@ -193,7 +193,6 @@ struct Status {
     int rebuild;      // 1: the lists are built in this evaluation
     unsigned disp2;   // largest squared displacement since the last build (float bits)
     int sticky;       // overflow bits of every build since the host last cleared them
-    int prep_done;    // CTAs of k_prepare done (the last one decides the list build)
 };
 
 // Arguments shared by the kernels of one engine (passed by value).
@@ -316,6 +315,7 @@ struct Args {
 };
 
 void launch_prepare(const Args& a, cudaStream_t s);
+void launch_decide(const Args& a, cudaStream_t s);
 void launch_find(const Args& a, cudaStream_t s);
 void launch_tiles(const Args& a, int grid, cudaStream_t s);
 void launch_find_tiles(const Args& a, cudaStream_t s);
