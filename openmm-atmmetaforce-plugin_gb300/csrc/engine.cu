@@ -1125,7 +1125,7 @@ void Engine::alloc_device() {
         for (int r = 0; r < R_; r++)
             rows = std::max(rows, (rep_host_[r].row1_e - rep_host_[r].row1_b) + (rep_host_[r].row2_e - rep_host_[r].row2_b));
         a.fin_ctas = std::min(64, std::max(1, (rows + 31) / 32));
-        a.fin_part = dalloc<unsigned long long>(d_allocs_, (size_t)R_ * a.fin_ctas * 2);
+        a.fin_part = dalloc<double>(d_allocs_, (size_t)R_ * a.fin_ctas * 2);
         a.fin_count = dalloc<int>(d_allocs_, (size_t)R_);
         CUDA_CHECK(cudaMemset(a.fin_count, 0, sizeof(int) * (size_t)R_));
     }

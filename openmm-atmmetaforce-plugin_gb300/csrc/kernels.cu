@@ -1060,17 +1060,16 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
 // Energies of a replica and the ATM merge, one kernel: CTA c of replica r sums
 // the tile energies of the replica's rows c, c + C, ... (C = fin_ctas; rows of
 // state 1, then rows of state 2 or of the difference tiles), warp per row, lanes
-// over its slots, as int64 fixed point (2^32 per kJ/mol: exact, order
-// independent sums, on the integer pipe rather than the narrow FP64 one), and
-// writes its two partials; the last CTA of the replica to finish (a counter it
-// resets for the next evaluation) adds the partials, the exceptions' and the
-// reciprocal sum's partials (FP64) and runs the FP64 merge.
+// over its slots, in FP64 and a fixed order (the difference tiles of a displaced
+// ligand that overlaps the solvent reach 1e10 kJ/mol and more, which the
+// soft-core exists to absorb: no fixed-point range is safe), and writes its two
+// partials; the last CTA of the replica to finish (a counter it resets for the
+// next evaluation) adds the partials in order, the exceptions' and the
+// reciprocal sum's partials, and runs the FP64 merge.
 constexpr int kFinThreads = 256;
 
-__device__ __forceinline__ long long fix_e(float v) { return (long long)fix_bits(v); }
-
 __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
-    __shared__ long long sh_i[2][kFinThreads / 32];
+    __shared__ double sh_r[2][kFinThreads / 32];
     __shared__ double sh[5][kFinThreads / 32];
     __shared__ int s_last;
     const int C = a.fin_ctas;
@@ -1078,15 +1077,15 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const RepDev& R = a.reps[r];
     const int n1 = R.row1_e - R.row1_b, n2 = R.row2_e - R.row2_b;
-    long long s1 = 0, s2 = 0;
+    double s1 = 0.0, s2 = 0.0;
     for (int k = c + C * w; k < n1 + n2; k += C * (kFinThreads / 32)) {
         const int row = k < n1 ? R.row1_b + k : R.row2_b + (k - n1);
         const int n = a.row_count[row];
         const float2* e = a.e_tile + (size_t)row * a.row_cap;
-        long long t = 0;
+        double t = 0.0;
         for (int q = lane; q < n; q += 32) {
             const float2 v = e[q];
-            t += fix_e(v.x) + fix_e(v.y);
+            t += (double)v.x + (double)v.y;
         }
         if (k < n1)
             s1 += t;
@@ -1099,18 +1098,18 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
         s2 += __shfl_xor_sync(FULL_MASK, s2, o);
     }
     if (lane == 0) {
-        sh_i[0][w] = s1;
-        sh_i[1][w] = s2;
+        sh_r[0][w] = s1;
+        sh_r[1][w] = s2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        long long t1 = 0, t2 = 0;
+        double t1 = 0.0, t2 = 0.0;
         for (int q = 0; q < kFinThreads / 32; q++) {
-            t1 += sh_i[0][q];
-            t2 += sh_i[1][q];
+            t1 += sh_r[0][q];
+            t2 += sh_r[1][q];
         }
-        a.fin_part[2 * (size_t)blockIdx.x] = (unsigned long long)t1;
-        a.fin_part[2 * (size_t)blockIdx.x + 1] = (unsigned long long)t2;
+        a.fin_part[2 * (size_t)blockIdx.x] = t1;
+        a.fin_part[2 * (size_t)blockIdx.x + 1] = t2;
         __threadfence();
         s_last = atomicAdd(&a.fin_count[r], 1) == C - 1;
     }
@@ -1138,18 +1137,17 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
     __syncthreads();
     if (threadIdx.x == 0) {
         a.fin_count[r] = 0;  // ready for the next evaluation
-        long long d1 = 0, d2 = 0;
-        const volatile unsigned long long* part = a.fin_part + 2 * (size_t)r * C;
+        double dir1 = 0.0, dir2 = 0.0;
+        const volatile double* part = a.fin_part + 2 * (size_t)r * C;
         for (int q = 0; q < C; q++) {
-            d1 += (long long)part[2 * q];
-            d2 += (long long)part[2 * q + 1];
+            dir1 += part[2 * q];
+            dir2 += part[2 * q + 1];
         }
         double t[5];
         for (int k = 0; k < 5; k++) {
             t[k] = 0.0;
             for (int q = 0; q < kFinThreads / 32; q++) t[k] += sh[k][q];
         }
-        const double dir1 = (double)d1 * (1.0 / 4294967296.0), dir2 = (double)d2 * (1.0 / 4294967296.0);
         const double x1 = t[0], x2 = t[1], xd = t[2], c1 = t[3], c2 = t[4];
         double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
         double E2;

@@ -263,7 +263,7 @@ struct Args {
     int* tile_j;              // 32 j slots per tile (atom tiles)
     float2* e_tile;           // nrows*row_cap: tile energies as (hi, lo) FP32 pairs, summed in FP64 per row
     int fin_ctas;             // finalize CTAs per replica (row sums), the last one merges
-    unsigned long long* fin_part;  // R x fin_ctas x 2: int64 fixed-point row-energy partials
+    double* fin_part;         // R x fin_ctas x 2: row-energy partials (state 1, state 2 / difference)
     int* fin_count;           // R: finalize CTAs done (the last resets it to 0)
     Status* status;
     // forces (fixed point), planes of NA: [F1x F1y F1z | F2x F2y F2z]

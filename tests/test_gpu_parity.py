@@ -245,6 +245,29 @@ def test_spreading_by_owner_gives_the_same_bits(diff):
         assert force_rel(F1[offs[k]:offs[k + 1]], ref["forces"]) <= F_TOL, k
 
 
+@pytest.mark.parametrize("diff", [0, 1], ids=["two-states", "difference"])
+def test_displaced_ligand_overlapping_a_water(diff):
+    """A ligand atom whose displaced position lies 0.05 nm from a water oxygen:
+    u reaches about 4e9 kJ/mol, beyond 2^31, in the range the soft-core exists to
+    absorb (an MD step can produce it).  The energies must be summed without a
+    range limit: u within 1e-4 relative of the oracle (a range limit shows as an
+    error of tens of percent; FP32 pair arithmetic gives about 3e-5 here, where
+    r^-12 multiplies the relative error of the hardware reciprocal square root
+    twelvefold), the soft-core perturbation energy within the usual tolerance.  (The pair's force, about 1e12 kJ/mol/nm,
+    is beyond the range of the fixed-point force sums, 2^31 kJ/mol/nm; the merge
+    weights it by sp, about 1e-10 here, and it is not compared.)"""
+    c = S.water_ligand_box(3000, 3.1, [16], [(1.4, 1.3, 1.5)], S.PME, 0.9, seed=44)
+    lig = np.nonzero(np.abs(c.displ).sum(axis=1) > 0)[0]
+    k = lig[len(lig) // 2]
+    c.pos[k] = c.pos[0] - c.displ[k] + np.array([0.05, 0.0, 0.0])  # atom 0 is a water oxygen
+    ref = O.atm_eval(c.spec, c.pos, c.displ, c.params)
+    assert ref["u"] > 2.0 ** 31
+    b = atm.ReplicaBatch([atm.system_from_case(c)[0]], 0, {"DifferencePath": diff})
+    E, F, r = b.evaluate(c.pos)
+    assert abs(r[0]["u"] - ref["u"]) <= 1e-4 * abs(ref["u"])
+    assert abs(r[0]["pert"] - ref["usc"]) <= U_TOL
+
+
 def test_batch_mixed_sizes_vs_oracle_and_matrix():
     cases = [S.abfe_pme_small(1500, 8, 21), S.abfe_pme_small(4000, 18, 22),
              S.abfe_pme_small(2500, 12, 23, displ=1.2), S.abfe_pme_small(6000, 30, 24)]
