@@ -1060,13 +1060,23 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
 // Energies of a replica and the ATM merge, one kernel: CTA c of replica r sums
 // the tile energies of the replica's rows c, c + C, ... (C = fin_ctas; rows of
 // state 1, then rows of state 2 or of the difference tiles), warp per row, lanes
-// over its slots, in FP64 and a fixed order (the difference tiles of a displaced
-// ligand that overlaps the solvent reach 1e10 kJ/mol and more, which the
-// soft-core exists to absorb: no fixed-point range is safe), and writes its two
+// over its slots, each lane in compensated FP32 (TwoSum: relative error of order
+// 2^-48 of the summed magnitudes, on the FP32 pipe) converted to FP64 once, then
+// FP64 across lanes and warps, in a fixed order (no fixed-point range would do:
+// the difference tiles of a displaced ligand that overlaps the solvent reach 1e10
+// kJ/mol and more, which the soft-core exists to absorb), and writes its two
 // partials; the last CTA of the replica to finish (a counter it resets for the
 // next evaluation) adds the partials in order, the exceptions' and the
 // reciprocal sum's partials, and runs the FP64 merge.
 constexpr int kFinThreads = 256;
+
+// Knuth's TwoSum: s + c carries the running sum exactly up to c's own rounding.
+__device__ __forceinline__ void fin_two_sum(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+}
 
 __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
     __shared__ double sh_r[2][kFinThreads / 32];
@@ -1077,21 +1087,24 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const RepDev& R = a.reps[r];
     const int n1 = R.row1_e - R.row1_b, n2 = R.row2_e - R.row2_b;
-    double s1 = 0.0, s2 = 0.0;
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;  // compensated sums of the two row kinds
     for (int k = c + C * w; k < n1 + n2; k += C * (kFinThreads / 32)) {
         const int row = k < n1 ? R.row1_b + k : R.row2_b + (k - n1);
         const int n = a.row_count[row];
         const float2* e = a.e_tile + (size_t)row * a.row_cap;
-        double t = 0.0;
+        const bool first = k < n1;
         for (int q = lane; q < n; q += 32) {
             const float2 v = e[q];
-            t += (double)v.x + (double)v.y;
+            if (first) {
+                fin_two_sum(h1, l1, v.x);
+                l1 += v.y;
+            } else {
+                fin_two_sum(h2, l2, v.x);
+                l2 += v.y;
+            }
         }
-        if (k < n1)
-            s1 += t;
-        else
-            s2 += t;
     }
+    double s1 = (double)h1 + (double)l1, s2 = (double)h2 + (double)l2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         s1 += __shfl_xor_sync(FULL_MASK, s1, o);
