@@ -191,7 +191,10 @@ int atm_system_set_position_restraints_periodic(atm_system_t sys, int periodic);
  * between them); SpreadByOwner=0|1 (default 1: PME charges spread once per atom,
  * by the grid brick that holds its stencil base, and the bricks summed into
  * integer grids; 0: every brick spreads each atom whose stencil touches it; the
- * grids, and so every result, are the same bits either way). */
+ * grids, and so every result, are the same bits either way); SpreadBrick=n (the
+ * spreading brick edge in grid points, 0: each atom's stencil added straight into
+ * the integer grid by atomics; the autotuner chooses among 20, 19, 16, 12 and 0;
+ * same bits in every case). */
 int atm_context_create(atm_system_t sys, int device, const char* properties, atm_context_t* out);
 int atm_context_destroy(atm_context_t ctx);
 /* Context::setPositions (host doubles, n x 3, nm). */
@@ -266,8 +269,8 @@ int atm_batch_backward(atm_batch_t b, const double* g, double* dx, double* dd, d
  * atm_md_autotune before the first step),
  * CheckInterval=steps (default 20: the host reads the list status every that
  * many steps instead of after every step, and redoes the steps since the last
- * check if a list build overflowed), FusedTiles=0|1 and SpreadByOwner=0|1 (as
- * for contexts).
+ * check if a list build overflowed), FusedTiles=0|1, SpreadByOwner=0|1 and
+ * SpreadBrick=n (as for contexts).
  * temperature K, friction 1/ps, step_size ps; seed keys the Philox4x32-10
  * thermostat noise. */
 typedef struct atm_md_s* atm_md_t;
