@@ -186,7 +186,9 @@ Engine::Engine(std::vector<ReplicaSpec> reps, int device, bool full_mode, bool a
                     throw Error(1, "The periodic box must be at least twice the cutoff in every dimension");
         if (s.method == NonbondedForce::PME)
             for (int a = 0; a < 3; a++)
-                if (s.grid[a] < 6) throw Error(1, "PME grid dimensions must be at least 6");
+                if (s.grid[a] < 6 || s.grid[a] > 1023)
+                    // (the spreading kernels pack a stencil's grid indices in 10 bits each)
+                    throw Error(1, "PME grid dimensions must be between 6 and 1023");
         for (const Exception& e : s.exc)
             if (e.i < 0 || e.j < 0 || e.i >= s.n || e.j >= s.n || e.i == e.j)
                 throw Error(2, "Exception particle index out of range");
