@@ -41,7 +41,8 @@ struct MdDev {
     const double* cent_w;
     const MdConsGroup* cons;
     const MdSettle* settle;
-    int n_bonds, n_angles, n_posres, n_cent, n_cons, n_settle;
+    const int* free_atoms;  // atoms in no constraint unit
+    int n_bonds, n_angles, n_posres, n_cent, n_cons, n_settle, n_free;
     const double* box;  // 6 per replica: ax, by, cz, bx, cx, cy (reduced box vectors)
     const int* rep_off; // R + 1
     double* ke;         // R
@@ -199,15 +200,13 @@ __device__ __forceinline__ void normals3(uint32_t i, uint32_t s0, uint32_t s1, u
     z[2] = (double)(b * c3f);
 }
 
-__global__ void k_md_integrate(MdDev a) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+// The Langevin update of atom i: the unconstrained new position xn from x, the
+// previous velocity, the forces and the thermostat noise (the velocity is set
+// from the constrained position afterwards, md_finish).
+__device__ __forceinline__ void md_integrate(const MdDev& a, int i, double* xn) {
     double im = a.inv_m[i];
     if (im == 0.0) {
-        for (int k = 0; k < 3; k++) {
-            a.v[3 * (size_t)i + k] = 0.0;
-            a.xn[3 * (size_t)i + k] = a.x[3 * (size_t)i + k];
-        }
+        for (int k = 0; k < 3; k++) xn[k] = a.x[3 * (size_t)i + k];
         return;
     }
     double z[3];
@@ -221,27 +220,25 @@ __global__ void k_md_integrate(MdDev a) {
         size_t o = 3 * (size_t)i + k;
         const double f = fma((double)(long long)a.fb[o], 1.0 / kFixScale, a.f_atm[o]);
         const double v = fma(nsim, z[k], fma(fim, f, a.vscale * a.v[o]));
-        a.v[o] = v;
-        a.xn[o] = fma(a.dt, v, a.x[o]);
+        xn[k] = fma(a.dt, v, a.x[o]);
     }
 }
 
-__global__ void k_md_shake(MdDev a) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= a.n_cons) return;
-    const MdConsGroup& c = a.cons[g];
-    double ref[kConsAtoms][3], p[kConsAtoms][3], im[kConsAtoms];
-    int na = 0;
-    for (int k = 0; k < kConsAtoms; k++) {
-        int i = c.atom[k];
-        if (i < 0) break;
-        na = k + 1;
-        im[k] = a.inv_m[i];
-        for (int d = 0; d < 3; d++) {
-            ref[k][d] = a.x[3 * (size_t)i + d];
-            p[k][d] = a.xn[3 * (size_t)i + d];
-        }
+// v = (x' - x) / dt and x <- x' for atom i (massless atoms keep v = 0).
+__device__ __forceinline__ void md_finish(const MdDev& a, double* x, int i, const double* xn) {
+    const double inv_dt = 1.0 / a.dt;
+    const bool massless = a.inv_m[i] == 0.0;
+    for (int k = 0; k < 3; k++) {
+        const size_t o = 3 * (size_t)i + k;
+        a.v[o] = massless ? 0.0 : (xn[k] - x[o]) * inv_dt;
+        x[o] = xn[k];
     }
+}
+
+// SHAKE iterations on one cluster: p (the unconstrained new positions) corrected
+// along the reference (pre-step) bonds; false when they did not converge.
+__device__ bool md_shake(const MdDev& a, const MdConsGroup& c, const double (*ref)[3], double (*p)[3],
+                         const double* im) {
     bool done = false;
     for (int it = 0; it < 1000 && !done; it++) {
         done = true;
@@ -264,9 +261,7 @@ __global__ void k_md_shake(MdDev a) {
             }
         }
     }
-    if (!done) atomicAdd(a.status, 1);
-    for (int k = 0; k < na; k++)
-        for (int d = 0; d < 3; d++) a.xn[3 * (size_t)c.atom[k] + d] = p[k][d];
+    return done;
 }
 
 __device__ __forceinline__ void cross3(const double* a, const double* b, double* c) {
@@ -286,19 +281,11 @@ __device__ __forceinline__ double dot3(const double* a, const double* b) {
 // new out-of-plane coordinates, then by theta (about Z) so that the in-plane
 // displacements are along the old bonds.
 
-__global__ void k_md_settle(MdDev a) {
-    int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= a.n_settle) return;
-    const MdSettle S = a.settle[w];
-    double a0[3], b0[3], c0[3], a1[3], b1[3], c1[3];
-    for (int d = 0; d < 3; d++) {
-        a0[d] = a.x[3 * (size_t)S.o + d];
-        b0[d] = a.x[3 * (size_t)S.h1 + d];
-        c0[d] = a.x[3 * (size_t)S.h2 + d];
-        a1[d] = a.xn[3 * (size_t)S.o + d];
-        b1[d] = a.xn[3 * (size_t)S.h1 + d];
-        c1[d] = a.xn[3 * (size_t)S.h2 + d];
-    }
+// SETTLE on one water: a0, b0, c0 the old positions of O, H1, H2; a1, b1, c1
+// their unconstrained new positions, replaced by the constrained ones; false (a1,
+// b1, c1 kept) when the displacement is too large for the closed form.
+__device__ bool md_settle(const MdSettle& S, const double* a0, const double* b0, const double* c0, double* a1,
+                          double* b1, double* c1) {
     double com[3], xa1[3], xb1[3], xc1[3], xb0[3], xc0[3];
     for (int d = 0; d < 3; d++) {
         com[d] = S.wo * a1[d] + S.wh * (b1[d] + c1[d]);
@@ -348,27 +335,57 @@ __global__ void k_md_settle(MdDev a) {
         rc3[d] = com[d] + pc[0] * X[d] + pc[1] * Y[d] + pc[2] * Z[d];
         ok = ok && isfinite(ra3[d]) && isfinite(rb3[d]) && isfinite(rc3[d]);
     }
-    if (!ok) {  // displacement too large for the closed form: leave the water, report
-        atomicAdd(a.status, 1);
-        return;
-    }
+    if (!ok) return false;  // displacement too large for the closed form: leave the water
     for (int d = 0; d < 3; d++) {
-        a.xn[3 * (size_t)S.o + d] = ra3[d];
-        a.xn[3 * (size_t)S.h1 + d] = rb3[d];
-        a.xn[3 * (size_t)S.h2 + d] = rc3[d];
+        a1[d] = ra3[d];
+        b1[d] = rb3[d];
+        c1[d] = rc3[d];
     }
+    return true;
 }
 
-__global__ void k_md_finish(MdDev a, double* x) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    double inv_dt = 1.0 / a.dt;
-    bool massless = a.inv_m[i] == 0.0;
-    for (int k = 0; k < 3; k++) {
-        size_t o = 3 * (size_t)i + k;
-        double xn = a.xn[o];
-        a.v[o] = massless ? 0.0 : (xn - x[o]) * inv_dt;
-        x[o] = xn;
+// One step's update, one thread per unit: a rigid water (the Langevin update of
+// its three atoms, SETTLE, the velocities from the constrained positions), a SHAKE
+// cluster (likewise), or an atom in no constraint; all in registers, one pass over
+// the state.  A failed constraint counts in the status and leaves its atoms at
+// their unconstrained positions.
+__global__ void k_md_update(MdDev a, double* x) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < a.n_settle) {
+        const MdSettle S = a.settle[u];
+        const int at[3] = {S.o, S.h1, S.h2};
+        double x0[3][3], x1[3][3];
+        for (int k = 0; k < 3; k++) {
+            for (int d = 0; d < 3; d++) x0[k][d] = a.x[3 * (size_t)at[k] + d];
+            md_integrate(a, at[k], x1[k]);
+        }
+        if (!md_settle(S, x0[0], x0[1], x0[2], x1[0], x1[1], x1[2])) atomicAdd(a.status, 1);
+        for (int k = 0; k < 3; k++) md_finish(a, x, at[k], x1[k]);
+        return;
+    }
+    const int g = u - a.n_settle;
+    if (g < a.n_cons) {
+        const MdConsGroup& c = a.cons[g];
+        double ref[kConsAtoms][3], p[kConsAtoms][3], im[kConsAtoms];
+        int na = 0;
+        for (int k = 0; k < kConsAtoms; k++) {
+            const int i = c.atom[k];
+            if (i < 0) break;
+            na = k + 1;
+            im[k] = a.inv_m[i];
+            for (int d = 0; d < 3; d++) ref[k][d] = a.x[3 * (size_t)i + d];
+            md_integrate(a, i, p[k]);
+        }
+        if (!md_shake(a, c, ref, p, im)) atomicAdd(a.status, 1);
+        for (int k = 0; k < na; k++) md_finish(a, x, c.atom[k], p[k]);
+        return;
+    }
+    const int f = g - a.n_cons;
+    if (f < a.n_free) {
+        const int i = a.free_atoms[f];
+        double xn[3];
+        md_integrate(a, i, xn);
+        md_finish(a, x, i, xn);
     }
 }
 
@@ -695,6 +712,17 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
         if (!water) shake_groups.push_back(g);
     }
     cons.swap(shake_groups);
+    std::vector<int> free_atoms;
+    {
+        std::vector<char> in_unit(n_, 0);
+        for (const MdSettle& w : settle) in_unit[w.o] = in_unit[w.h1] = in_unit[w.h2] = 1;
+        for (const MdConsGroup& g : cons)
+            for (int k = 0; k < kConsAtoms; k++)
+                if (g.atom[k] >= 0) in_unit[g.atom[k]] = 1;
+        for (int i = 0; i < n_; i++)
+            if (!in_unit[i]) free_atoms.push_back(i);
+    }
+    n_free_ = (int)free_atoms.size();
     rep_off[R_] = n_;
     n_bonds_ = (int)bonds.size();
     n_angles_ = (int)angles.size();
@@ -730,6 +758,7 @@ void MDDriver::upload_terms(const std::vector<const System*>& systems) {
     cent_w_ = md_upload(allocs_, cent_w);
     cons_ = md_upload(allocs_, cons);
     settle_ = md_upload(allocs_, settle);
+    free_ = md_upload(allocs_, free_atoms);
     box_d_ = md_upload(allocs_, box);
     rep_off_d_ = md_upload(allocs_, rep_off);
     ke_d_ = md_alloc<double>(allocs_, R_);
@@ -759,6 +788,8 @@ MdDev MDDriver::dev_args() const {
     a.cent_w = cent_w_;
     a.cons = cons_;
     a.settle = settle_;
+    a.free_atoms = free_;
+    a.n_free = n_free_;
     a.n_bonds = n_bonds_;
     a.n_angles = n_angles_;
     a.n_posres = n_posres_;
@@ -957,11 +988,8 @@ void MDDriver::step(int nsteps) {
         if (!forces_valid_) compute_forces(false);
         record_step();
         MdDev a = dev_args();
-        int nb = (n_ + 255) / 256;
-        k_md_integrate<<<nb, 256, 0, s_>>>(a);
-        if (n_cons_ > 0) k_md_shake<<<(n_cons_ + 127) / 128, 128, 0, s_>>>(a);
-        if (n_settle_ > 0) k_md_settle<<<(n_settle_ + 127) / 128, 128, 0, s_>>>(a);
-        k_md_finish<<<nb, 256, 0, s_>>>(a, x_);
+        const int units = n_settle_ + n_cons_ + n_free_;
+        if (units > 0) k_md_update<<<(units + 127) / 128, 128, 0, s_>>>(a, x_);
         MD_CHECK(cudaGetLastError());
         step_++;
         k++;

@@ -161,6 +161,7 @@ private:
     double* cent_w_ = nullptr;
     MdConsGroup* cons_ = nullptr;
     MdSettle* settle_ = nullptr;
+    int* free_ = nullptr;      // atoms in no constraint unit
     double* box_d_ = nullptr;  // 3 per replica
     int* rep_off_d_ = nullptr; // R + 1
     double* ke_d_ = nullptr;   // R
@@ -168,7 +169,7 @@ private:
     long long step_snap_ = 0, rec_count_snap_ = 0, rec_last_snap_ = -1;
     int checks_ = 0, redos_ = 0;
     bool tuned_ = false;
-    int n_bonds_ = 0, n_angles_ = 0, n_posres_ = 0, n_cent_ = 0, n_cons_ = 0, n_settle_ = 0;
+    int n_bonds_ = 0, n_angles_ = 0, n_posres_ = 0, n_cent_ = 0, n_cons_ = 0, n_settle_ = 0, n_free_ = 0;
     std::vector<int> term_rep_;  // replica of each term, in e_terms_ order
     // recording
     int rec_interval_ = 0, rec_cap_ = 0;
