@@ -263,7 +263,7 @@ def md_bench(cases_fn, R, steps, warmup, device, record_interval=0):
     sim.step(MD_SETTINGS["thermalise_steps"])
     integ.setFriction(MD_SETTINGS["friction_per_ps"])
     # launch configuration and pair-list skin chosen by the autotuner (state restored after)
-    tune = sim.autotune(trials=20).strip().splitlines()
+    tune = sim.autotune(trials=60).strip().splitlines()  # 60 timed steps per skin: steadier choice
     sim.step(warmup)
     if record_interval:
         sim.setRecording(record_interval, capacity=steps // record_interval + 1)
