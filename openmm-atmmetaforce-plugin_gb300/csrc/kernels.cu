@@ -1061,8 +1061,9 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
 // the tile energies of the replica's rows c, c + C, ... (C = fin_ctas; rows of
 // state 1, then rows of state 2 or of the difference tiles), warp per row, lanes
 // over its slots, each lane in compensated FP32 (TwoSum: relative error of order
-// 2^-48 of the summed magnitudes, on the FP32 pipe) converted to FP64 once, then
-// FP64 across lanes and warps, in a fixed order (no fixed-point range would do:
+// 2^-48 of the summed magnitudes, on the FP32 pipe), the lanes' compensated pairs
+// combined over a shuffle tree and converted to FP64 once per warp, then FP64
+// across warps and CTAs, in a fixed order (no fixed-point range would do:
 // the difference tiles of a displaced ligand that overlaps the solvent reach 1e10
 // kJ/mol and more, which the soft-core exists to absorb), and writes its two
 // partials; the last CTA of the replica to finish (a counter it resets for the
@@ -1076,6 +1077,17 @@ __device__ __forceinline__ void fin_two_sum(float& s, float& c, float x) {
     const float bp = t - s;
     c += (s - (t - bp)) + (x - bp);
     s = t;
+}
+
+// (h, l) += (hb, lb) for two compensated sums: TwoSum of the leading parts, the
+// trailing parts added to its error, renormalised (Fast2Sum) so that the next
+// combination's TwoSum sees the full leading part.
+__device__ __forceinline__ void fin_pair_add(float& h, float& l, float hb, float lb) {
+    const float s = h + hb;
+    const float bp = s - h;
+    const float t = ((h - (s - bp)) + (hb - bp)) + (l + lb);
+    h = s + t;
+    l = t - (h - s);
 }
 
 __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
@@ -1104,15 +1116,17 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
             }
         }
     }
-    double s1 = (double)h1 + (double)l1, s2 = (double)h2 + (double)l2;
+    // across the warp as compensated pairs on the FP32 pipe, to FP64 once per warp
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        s1 += __shfl_xor_sync(FULL_MASK, s1, o);
-        s2 += __shfl_xor_sync(FULL_MASK, s2, o);
+        const float hb1 = __shfl_xor_sync(FULL_MASK, h1, o), lb1 = __shfl_xor_sync(FULL_MASK, l1, o);
+        const float hb2 = __shfl_xor_sync(FULL_MASK, h2, o), lb2 = __shfl_xor_sync(FULL_MASK, l2, o);
+        fin_pair_add(h1, l1, hb1, lb1);
+        fin_pair_add(h2, l2, hb2, lb2);
     }
     if (lane == 0) {
-        sh_r[0][w] = s1;
-        sh_r[1][w] = s2;
+        sh_r[0][w] = (double)h1 + (double)l1;
+        sh_r[1][w] = (double)h2 + (double)l2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1148,19 +1162,31 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(Args a) {
         if (lane == 0) sh[k][w] = v[k];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        a.fin_count[r] = 0;  // ready for the next evaluation
-        double dir1 = 0.0, dir2 = 0.0;
+    if (w != 0) return;
+    // warp 0: the CTAs' partials (lane q holds CTAs q, q + 32, ...) and the warps'
+    // sums, each added over a fixed shuffle tree
+    double dir1 = 0.0, dir2 = 0.0;
+    {
         const volatile double* part = a.fin_part + 2 * (size_t)r * C;
-        for (int q = 0; q < C; q++) {
+        for (int q = lane; q < C; q += 32) {
             dir1 += part[2 * q];
             dir2 += part[2 * q + 1];
         }
-        double t[5];
-        for (int k = 0; k < 5; k++) {
-            t[k] = 0.0;
-            for (int q = 0; q < kFinThreads / 32; q++) t[k] += sh[k][q];
-        }
+    }
+    double t[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) t[k] = lane < kFinThreads / 32 ? sh[k][lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dir1 += __shfl_xor_sync(FULL_MASK, dir1, o);
+        dir2 += __shfl_xor_sync(FULL_MASK, dir2, o);
+    }
+#pragma unroll
+    for (int o = (kFinThreads / 32) / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 5; k++) t[k] += __shfl_xor_sync(FULL_MASK, t[k], o);
+    if (lane == 0) {
+        a.fin_count[r] = 0;  // ready for the next evaluation
         const double x1 = t[0], x2 = t[1], xd = t[2], c1 = t[3], c2 = t[4];
         double E1 = dir1 + x1 + c1 + R.e_self + R.e_disp;
         double E2;
