@@ -74,8 +74,19 @@ __global__ void k_prepare(Args a) {
     if (o < 0) o = a.orig[b * kTile];  // padding copies the block's first atom
     const double* p = (a.io[0] ? a.io[0] : a.pos_in) + 3 * (size_t)(R.in_off + o);
     double xd = p[0], yd = p[1], zd = p[2];
-    wrap3d(xd, yd, zd, R);  // FP64 wrap into the unit cell
     float x = (float)xd, y = (float)yd, z = (float)zd;
+    // a position whose reduced coordinates lie safely inside (0, 1) (by 1e-5, far
+    // beyond the FP32 estimate's error) is in the unit cell already: the FP64 wrap
+    // would subtract zero.  Others take the FP64 wrap (FP64 is 1/64 of the FP32
+    // rate on this part).
+    constexpr float kIn = 1e-5f;
+    const float ux = x * R.ibox[0], uy = y * R.ibox[1], uz = z * R.ibox[2];
+    if (!(ux >= kIn && ux <= 1.0f - kIn && uy >= kIn && uy <= 1.0f - kIn && uz >= kIn && uz <= 1.0f - kIn)) {
+        wrap3d(xd, yd, zd, R);  // FP64 wrap into the unit cell
+        x = (float)xd;
+        y = (float)yd;
+        z = (float)zd;
+    }
     float q = a.qs[s];
     a.posq[s] = make_float4(x, y, z, q);
     if (a.skin_half2 > 0.f) {
