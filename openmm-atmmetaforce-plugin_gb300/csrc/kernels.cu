@@ -1241,13 +1241,21 @@ __global__ void __launch_bounds__(kOutThreads) k_output(Args a) {
         const double* res = a.results + (size_t)rep * NUM_RES;
         const double sp = res[RES_SP];
         const double wgt = R.params[8] > 0 ? sp : 1.0 - sp;
+        // F1 + w (F2 - F1) in the fixed point of the force sums, w in units of 2^-32
+        // (w in [0, 1]: at most 2^32; its rounding is 2^-33 relative to F2 - F1),
+        // the product by a 128-bit multiply (floor), then one conversion per
+        // component and the exact 2^-32 scaling in the exponent field
+        const long long w32 = __double2ll_rn(wgt * 4294967296.0);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const long long f1 = (long long)a.F[(size_t)k * a.NA + s];
             const long long f2 = (long long)a.F[(size_t)(3 + k) * a.NA + s];
-            const double d = a.full ? (double)(f2 - f1) : (double)f2;
-            f[k] = R.var_nb ? ((double)f1 + wgt * d) * (1.0 / kFixScale) : 0.0;
-            if (a.f_nb) a.f_nb[3 * (size_t)g + k] = (double)f1 * (1.0 / kFixScale);
+            const long long d = a.full ? f2 - f1 : f2;
+            const long long hi = __mul64hi(d, w32);
+            const unsigned long long lo = (unsigned long long)d * (unsigned long long)w32;
+            const long long v = f1 + (long long)(((unsigned long long)hi << 32) | (lo >> 32));
+            f[k] = R.var_nb ? fix_scaled(v) : 0.0;
+            if (a.f_nb) a.f_nb[3 * (size_t)g + k] = fix_scaled(f1);
         }
     }
     const int g0 = g - lane;  // the warp's first atom

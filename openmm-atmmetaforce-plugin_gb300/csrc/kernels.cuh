@@ -32,6 +32,13 @@ __device__ __forceinline__ unsigned long long fix_bits(float v) {
     const unsigned hi = (unsigned)__float2int_rz(h);
     return ((unsigned long long)hi << 32) | lo;
 }
+
+// v 2^-32 as a double (a fixed-point force sum in kJ/mol/nm): one conversion, then
+// the exact scaling by 2^-32 as an exponent decrement (|v| >= 1 stays normal).
+__device__ __forceinline__ double fix_scaled(long long v) {
+    const double d = (double)v;
+    return v == 0 ? 0.0 : __longlong_as_double(__double_as_longlong(d) - (32LL << 52));
+}
 #endif
 
 // The z-row stride (words) of a spreading brick's int32 accumulator: at least n,
