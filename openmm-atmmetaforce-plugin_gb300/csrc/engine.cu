@@ -710,11 +710,19 @@ void Engine::build_layout() {
         }
         rd.row2_e = (int)row_desc_.size();
     }
-    // Few rows (one or two replicas): each row's candidate blocks are split over
-    // up to 4 warps (parts), so that the list building is not one row's latency.
+    // Few rows for the finder's resident warps: each row's candidate blocks are
+    // split over up to 4 warps (parts: the warps per row, and 2 while the rows are
+    // fewer than twice the warps), so that the list building is not the latency of
+    // a few long rows (the difference rows scan every block of their replica).
+    // Measured on subsets of the 22 x 23,558-atom batch: 4 replicas 11,800 -> 14,300
+    // evaluations/s (2 parts instead of 1), 5 replicas 12,400 -> 14,900, 8 replicas
+    // 16,400 -> 17,600; two parts at 11 and 22 replicas lost 3-4 %, and 3 parts
+    // in place of 2 at 2 replicas lost 4 %.
     {
         const int base_rows = (int)row_desc_.size();
-        int parts = base_rows > 0 ? sms_ * find_warps_per_sm() / base_rows : 1;
+        const int warps = sms_ * find_warps_per_sm();
+        int parts = base_rows > 0 ? warps / base_rows : 1;
+        if (parts <= 1 && 2 * warps > base_rows) parts = 2;
         parts = std::max(1, std::min(4, parts));
         if (parts > 1) {
             std::vector<int4> split;
