@@ -1017,12 +1017,15 @@ __device__ double softcore(double u, double umax, double acore, double ub, doubl
         fp = 1.0;
         return u;
     }
+    // (one thread per replica runs this FP64 chain, whose latency the evaluation
+    // waits on: zeta^acore as exp(acore log zeta), 1/(1 + zeta^acore) taken once)
     double gu = (u - ub) / (acore * (umax - ub));
     double zeta = 1.0 + 2.0 * gu * (gu + 1.0);
-    double zetap = pow(zeta, acore);
+    double zetap = exp(acore * log(zeta));
     double sf = 4.0 * (2.0 * gu + 1.0) / zeta;
-    fp = sf * zetap / ((1.0 + zetap) * (1.0 + zetap));
-    return (umax - ub) * (zetap - 1.0) / (zetap + 1.0) + ub;
+    const double rz = 1.0 / (1.0 + zetap);
+    fp = sf * zetap * rz * rz;
+    return (umax - ub) * (zetap - 1.0) * rz + ub;
 }
 
 // The merge of ReferenceATMMetaForceKernels.cpp:82-98 plus the closed-form
@@ -1036,11 +1039,12 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
     double usc = softcore(u, umax, acore, ub, fp);
     double x = exp(-alpha * (usc - u0));
     double ee = 1.0 + x;
+    const double iee = 1.0 / ee, ia = alpha > 0 ? 1.0 / alpha : 0.0;
     double W = 0.0;
     double L = log(ee);
-    if (alpha > 0) W = ((l2 - l1) / alpha) * L;
+    if (alpha > 0) W = ((l2 - l1) * ia) * L;
     W += l2 * usc + w0;
-    double bfp = (l2 - l1) / ee + l1;
+    double bfp = (l2 - l1) * iee + l1;
     out[RES_ENERGY] = e0 + W;
     out[RES_PERT] = usc;
     out[RES_SP] = bfp * fp;
@@ -1052,10 +1056,10 @@ __device__ void atm_merge(double E1, double E2, const double* p, double* out) {
     out[RES_E1] = E1;
     out[RES_E2] = E2;
     if (alpha > 0) {
-        out[RES_DL1] = -L / alpha;
-        out[RES_DL2] = L / alpha + usc;
-        out[RES_DALPHA] = -(l2 - l1) / (alpha * alpha) * L - (l2 - l1) / alpha * (usc - u0) * x / ee;
-        out[RES_DU0] = (l2 - l1) * x / ee;
+        out[RES_DL1] = -L * ia;
+        out[RES_DL2] = L * ia + usc;
+        out[RES_DALPHA] = -(l2 - l1) * (ia * ia) * L - (l2 - l1) * ia * (usc - u0) * x * iee;
+        out[RES_DU0] = (l2 - l1) * x * iee;
     } else {
         out[RES_DL1] = 0.0;
         out[RES_DL2] = usc;
